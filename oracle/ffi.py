@@ -1,0 +1,280 @@
+"""ctypes access to the CPU oracle and to the reference built for the CPU.
+
+TEST INFRASTRUCTURE ONLY.  Loads
+  oracle/_build/libmpres_oracle.so   the C restatement (builds with `make -C oracle`)
+  oracle/_ref/libmpres_ref_<N>.so    the reference compiled here (oracle/ref/build_ref.sh),
+                                     present only where the reference checkout exists.
+Numbers travel as numpy structured arrays in the reference's mp_float_t layout.
+"""
+import ctypes
+import os
+import pathlib
+import subprocess
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "libmpres_oracle.so"
+REF_DIR = HERE / "_ref"
+
+ER = np.dtype([("frac", "<f8"), ("exp", "<i8")])
+P = ctypes.c_void_p
+MBLAS_NO_TRANS, MBLAS_TRANS = 111, 112
+
+
+def mp_dtype(n):
+    """mp_float_t of the reference (src/types.cuh:69-74) for n moduli: 4n + 40 bytes."""
+    dt = np.dtype([("digits", "<i4", (n,)), ("sign", "<i4"), ("exp", "<i4"), ("eval", ER, (2,))])
+    assert dt.itemsize == 4 * n + 40
+    return dt
+
+
+def ptr(a):
+    return a.ctypes.data_as(P)
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+
+
+_oracle = None
+
+
+def oracle():
+    """The C oracle (built on first use)."""
+    global _oracle
+    if _oracle is None:
+        if not ORACLE_SO.exists():
+            build_oracle()
+        lib = ctypes.CDLL(str(ORACLE_SO))
+        lib.ora_init.restype = P
+        _oracle = Oracle(lib)
+    return _oracle
+
+
+class _Common:
+    """Wrappers shared by the oracle and the reference library."""
+
+    def __init__(self, lib, prefix):
+        self.lib = lib
+        self.p = prefix
+
+    def _f(self, name):
+        return getattr(self.lib, self.p + name)
+
+
+class Oracle(_Common):
+    def __init__(self, lib):
+        super().__init__(lib, "ora_")
+
+    def threads(self):
+        return self.lib.ora_threads()
+
+    def set_d(self, n, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(x.size, mp_dtype(n))
+        self.lib.ora_set_d(n, ptr(x), ctypes.c_long(x.size), ptr(out))
+        return out
+
+    def tables(self, n, log2m):
+        return _tables(lambda *a: self.lib.ora_tables(n, *a), n, log2m)
+
+    def add(self, n, x, y):
+        r = np.zeros(len(x), mp_dtype(n))
+        self.lib.ora_add(n, ptr(x), ptr(y), ptr(r), ctypes.c_long(len(x)))
+        return r
+
+    def mul(self, n, x, y):
+        r = np.zeros(len(x), mp_dtype(n))
+        self.lib.ora_mul(n, ptr(x), ptr(y), ptr(r), ctypes.c_long(len(x)))
+        return r
+
+    def mul_d(self, n, x, d):
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        r = np.zeros(len(x), mp_dtype(n))
+        self.lib.ora_mul_d(n, ptr(x), ptr(d), ptr(r), ctypes.c_long(len(x)))
+        return r
+
+    def eval_fast(self, n, digits):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        cnt = digits.size // n
+        lo, up = np.zeros(cnt, ER), np.zeros(cnt, ER)
+        self.lib.ora_eval_fast(n, ptr(digits), ptr(lo), ptr(up), ctypes.c_long(cnt))
+        return lo, up
+
+    def eval(self, n, digits):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        cnt = digits.size // n
+        lo, up = np.zeros(cnt, ER), np.zeros(cnt, ER)
+        self.lib.ora_eval(n, ptr(digits), ptr(lo), ptr(up), ctypes.c_long(cnt))
+        return lo, up
+
+    def scale2pow(self, n, digits, D):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        D = np.ascontiguousarray(D, dtype=np.uint32)
+        out = np.zeros_like(digits)
+        self.lib.ora_scale2pow(n, ptr(digits), ptr(D), ptr(out), ctypes.c_long(D.size))
+        return out
+
+    def dot(self, n, x, y, g3=256, b3=64, incx=1, incy=1, length=None):
+        length = len(x) if length is None else length
+        r = np.zeros(1, mp_dtype(n))
+        self.lib.ora_dot(n, length, ptr(x), incx, ptr(y), incy, ptr(r), g3, b3)
+        return r
+
+    def gemv(self, n, trans, m, cols, alpha, A, lda, x, beta, y, incx=1, incy=1, b3=32):
+        y = y.copy()
+        self.lib.ora_gemv(n, trans, m, cols, ptr(alpha), ptr(A), lda, ptr(x), incx, ptr(beta), ptr(y), incy, b3)
+        return y
+
+    def gemm(self, n, m, cols, k, alpha, A, lda, B, ldb, beta, C, ldc):
+        C = C.copy()
+        self.lib.ora_gemm(n, m, cols, k, ptr(alpha), ptr(A), lda, ptr(B), ldb, ptr(beta), ptr(C), ldc)
+        return C
+
+    def spmv_csr(self, n, m, irp, ja, vals, x):
+        y = np.zeros(m, mp_dtype(n))
+        self.lib.ora_spmv_csr(n, m, ptr(irp), ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+    def spmv_csrv(self, n, m, tpr, irp, ja, vals, x):
+        y = np.zeros(m, mp_dtype(n))
+        self.lib.ora_spmv_csrv(n, m, tpr, ptr(irp), ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+    def spmv_ell(self, n, m, maxnzr, ja, vals, x):
+        y = np.zeros(m, mp_dtype(n))
+        self.lib.ora_spmv_ell(n, m, maxnzr, ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+
+def _tables(fn, n, log2m):
+    t = dict(
+        part_inv=np.zeros(n, np.int32),
+        pow2=np.zeros((log2m + 1) * n, np.int32),
+        m_pow2_res=np.zeros(30, np.int32),
+        part_pow2_res=np.zeros(30 * n, np.int32),
+        pow2_inv=np.zeros(30 * n, np.int32),
+        recip_rd=np.zeros(n, np.float64),
+        recip_ru=np.zeros(n, np.float64),
+        mrc_inv=np.zeros(n * n, np.int32),
+        eval_acc=np.zeros(1, np.float64),
+        ref_factor=np.zeros(1, np.int32),
+        units=np.zeros(4, ER),
+        mp_consts=np.zeros(3, np.int32),
+    )
+    fn(*[ptr(v) for v in t.values()])
+    return t
+
+
+_refs = {}
+
+
+def ref_available(n=8):
+    return (REF_DIR / ("libmpres_ref_%d.so" % n)).exists()
+
+
+class Reference(_Common):
+    """The reference library compiled for the CPU (one moduli set per library)."""
+
+    def __init__(self, n):
+        lib = ctypes.CDLL(str(REF_DIR / ("libmpres_ref_%d.so" % n)))
+        super().__init__(lib, "ref_")
+        assert lib.ref_moduli_size() == n
+        self.n = n
+        lib.ref_init()
+
+    def set_d(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(x.size, mp_dtype(self.n))
+        self.lib.ref_set_d(ptr(x), ctypes.c_long(x.size), ptr(out))
+        return out
+
+    def tables(self, log2m):
+        return _tables(self.lib.ref_tables, self.n, log2m)
+
+    def _elem(self, name, x, y):
+        r = np.zeros(len(x), mp_dtype(self.n))
+        getattr(self.lib, name)(ptr(x), ptr(y), ptr(r), ctypes.c_long(len(x)))
+        return r
+
+    def add(self, x, y):
+        return self._elem("ref_dev_add", x, y)
+
+    def mul(self, x, y):
+        return self._elem("ref_dev_mul", x, y)
+
+    def mul_d(self, x, d):
+        return self._elem("ref_dev_mul_d", x, np.ascontiguousarray(d, dtype=np.float64))
+
+    def eval_fast(self, digits):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        cnt = digits.size // self.n
+        lo, up = np.zeros(cnt, ER), np.zeros(cnt, ER)
+        self.lib.ref_dev_eval_fast(ptr(digits), ptr(lo), ptr(up), ctypes.c_long(cnt))
+        return lo, up
+
+    def eval(self, digits):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        cnt = digits.size // self.n
+        lo, up = np.zeros(cnt, ER), np.zeros(cnt, ER)
+        self.lib.ref_dev_eval(ptr(digits), ptr(lo), ptr(up), ctypes.c_long(cnt))
+        return lo, up
+
+    def scale2pow(self, digits, D):
+        digits = np.ascontiguousarray(digits, dtype=np.int32)
+        D = np.ascontiguousarray(D, dtype=np.uint32)
+        out = np.zeros_like(digits)
+        self.lib.ref_dev_scale2pow(ptr(digits), ptr(D), ptr(out), ctypes.c_long(D.size))
+        return out
+
+    def dot(self, x, y, g1=512, b1=128, g2=8192, g3=256, b3=64, incx=1, incy=1, length=None):
+        length = len(x) if length is None else length
+        r = np.zeros(1, mp_dtype(self.n))
+        self.lib.ref_dot(length, ptr(x), incx, ptr(y), incy, ptr(r), g1, b1, g2, g3, b3)
+        return r
+
+    def gemv(self, trans, m, cols, alpha, A, lda, x, beta, y, incx=1, incy=1, g1=256, b1=128, g2=256, b3=32):
+        y = y.copy()
+        self.lib.ref_gemv(trans, m, cols, ptr(alpha), ptr(A), lda, ptr(x), incx, ptr(beta), ptr(y), incy,
+                          g1, b1, g2, b3)
+        return y
+
+    def gemm(self, m, cols, k, alpha, A, lda, B, ldb, beta, C, ldc, b1x=32, b1y=1, g2x=128, g2y=64, b3=16):
+        C = C.copy()
+        self.lib.ref_gemm(m, cols, k, ptr(alpha), ptr(A), lda, ptr(B), ldb, ptr(beta), ptr(C), ldc,
+                          b1x, b1y, g2x, g2y, b3)
+        return C
+
+    def spmv_csr(self, m, irp, ja, vals, x):
+        y = np.zeros(m, mp_dtype(self.n))
+        self.lib.ref_spmv_csr(m, ptr(irp), ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+    def spmv_csrv(self, m, tpr, irp, ja, vals, x):
+        y = np.zeros(m, mp_dtype(self.n))
+        self.lib.ref_spmv_csrv(m, tpr, ptr(irp), ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+    def spmv_ell(self, m, maxnzr, ja, vals, x):
+        y = np.zeros(m, mp_dtype(self.n))
+        self.lib.ref_spmv_ell(m, maxnzr, ptr(ja), ptr(vals), ptr(x), ptr(y))
+        return y
+
+
+def reference(n):
+    if n not in _refs:
+        _refs[n] = Reference(n)
+    return _refs[n]
+
+
+def same_bits(a, b):
+    """Bitwise equality of two mp_float_t arrays (digits, sign, exp and eval)."""
+    return a.tobytes() == b.tobytes()
+
+
+def mismatches(a, b):
+    """Indices where two mp_float_t arrays differ in any byte."""
+    av = a.view(np.uint8).reshape(len(a), -1)
+    bv = b.view(np.uint8).reshape(len(b), -1)
+    return np.nonzero((av != bv).any(axis=1))[0]
