@@ -1,0 +1,177 @@
+/*
+ * mpres_gb300: GB300-native RNS multiple-precision BLAS hot path.
+ *
+ * C ABI of libmpres_gb300.so.  Every entry point takes plain pointers and sizes
+ * and replaces one interface of MPRES-BLAS (cited per function as
+ * reference-file:line).  The data types keep the reference's memory layouts
+ * (src/types.cuh:46-131), so arrays built by reference code can be passed as-is.
+ *
+ * Moduli sets.  The reference fixes one set per build through src/params.h.
+ * This library holds the predefined 32-bit sets of 8, 16 and 32 moduli at once;
+ * every call names its set by `nmod` (the reference's RNS_MODULI_SIZE), and an
+ * mp_float_t of that set is 4*nmod + 40 bytes.  include/mpres_gb300.hpp wraps
+ * these functions in the reference's own C++ names and template signatures.
+ *
+ * Errors.  The reference returns nothing and prints CUDA errors
+ * (src/common.cuh:38-53).  Every function here returns MPRES_SUCCESS or an
+ * error code; mpres_last_error() describes the last failure of this thread.
+ * Invalid sizes or strides that the reference silently ignores are ignored
+ * here too (MPRES_SUCCESS, nothing computed), with the same tests.
+ *
+ * Streams.  `stream` is a cudaStream_t (NULL = the legacy default stream).
+ * Computations are asynchronous with respect to the host, like the reference's
+ * kernel launches; the copy helpers are synchronous like the reference's.
+ *
+ * Inputs must hold canonical residues (0 <= digit < modulus), as every array
+ * produced by the reference's and this library's conversions does.
+ */
+#ifndef MPRES_GB300_H
+#define MPRES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- types, identical in layout to src/types.cuh:46-131 ---------------- */
+#ifndef MPRES_REFERENCE_TYPES_DEFINED
+#define MPRES_REFERENCE_TYPES_DEFINED
+typedef struct {
+    double frac; /* significand */
+    long exp;    /* exponent, base 2 */
+} er_float_t;
+
+typedef struct { int x, y, z, w; } mpres_int4;
+
+/* SoA multiple-precision array: digits element-major ([x0 residues][x1 residues]...),
+ * sign[len], exp[len], eval[2*len] = [lower bounds][upper bounds], buf[len], and
+ * len = DEVICE pointer to the element count. */
+typedef struct {
+    int *digits;
+    int *sign;
+    int *exp;
+    er_float_t *eval;
+    mpres_int4 *buf;
+    int *len;
+} mp_array_t;
+
+typedef struct {
+    double *as; /* nonzeros, row-major */
+    int *ja;    /* column indices */
+    int *irp;   /* row start pointers, m + 1 entries */
+} csr_t;
+
+typedef struct {
+    double *as; /* m * maxnzr slots, column-major, zero padded */
+    int *ja;
+} ell_t;
+#endif
+
+enum mpres_status {
+    MPRES_SUCCESS = 0,
+    MPRES_ERR_INVALID_VALUE = 1, /* unsupported moduli set or argument */
+    MPRES_ERR_NOT_INITIALIZED = 2,
+    MPRES_ERR_CUDA = 3,          /* a CUDA runtime call or a kernel launch failed */
+    MPRES_ERR_NOT_SUPPORTED = 4  /* e.g. a transposed mp_gemm (the reference prints and returns) */
+};
+
+/* mblas_trans_type values of src/blas/mblas_enum.cuh:25-29 */
+#define MPRES_NO_TRANS 111
+#define MPRES_TRANS 112
+#define MPRES_CONJ_TRANS 113
+
+/* Last error of the calling host thread, or "" after a success. */
+const char *mpres_last_error(void);
+
+/* Bytes of one mp_float_t of the given set (4*nmod + 40), 0 if unsupported. */
+size_t mpres_mp_float_size(int nmod);
+
+/* Replaces rns_const_init() (src/rns.cuh:324-442) and mp_const_init()
+ * (src/arith/arith_utils.cuh:44-90): computes the set's constants and places
+ * them on the current device.  Idempotent; must precede any other call of the
+ * set on that device. */
+int mpres_init(int nmod);
+
+/* Integer constants of the set: out[0] = MP_PRECISION, out[1] = MP_H,
+ * out[2] = MP_J, out[3] = RNS_EVAL_REF_FACTOR, out[4] = RNS_MODULI_PRODUCT_LOG2. */
+int mpres_get_int_constants(int nmod, int *out);
+
+/* ---- containers (src/mparray.cuh:35-160, src/sparse/utils/*.cuh) -------- */
+
+/* cuda::mp_array_init (src/mparray.cuh:35-56): allocates the six device arrays. */
+int mpres_array_init(int nmod, mp_array_t *a, size_t size);
+/* cuda::mp_array_clear (src/mparray.cuh:59-68). */
+int mpres_array_clear(mp_array_t *a);
+/* cuda::mp_array_host2device (src/mparray.cuh:76-118): host mp_float_t[size] ->
+ * device SoA, packed on the host and sent with four bulk copies. */
+int mpres_array_host2device(int nmod, mp_array_t *dst, const void *host_src, size_t size);
+/* cuda::mp_array_device2host (src/mparray.cuh:125-160). */
+int mpres_array_device2host(int nmod, void *host_dst, const mp_array_t *src, size_t size);
+
+/* cuda::csr_init / csr_host2device / csr_clear (src/sparse/utils/csr_utils.cuh:58-78). */
+int mpres_csr_init(csr_t *csr, int m, int nnz);
+int mpres_csr_host2device(csr_t *dev, const csr_t *host, int m, int nnz);
+int mpres_csr_clear(csr_t *csr);
+/* cuda::ell_init / ell_host2device / ell_clear (src/sparse/utils/ell_utils.cuh:55-71). */
+int mpres_ell_init(ell_t *ell, int m, int maxnzr);
+int mpres_ell_host2device(ell_t *dev, const ell_t *host, int m, int maxnzr);
+int mpres_ell_clear(ell_t *ell);
+
+/* ---- conversion --------------------------------------------------------- */
+
+/* mp_set_d (src/arith/assign.cuh:54-81), host: x[count] -> mp_float_t[count]. */
+int mpres_set_d(int nmod, const double *x, size_t count, void *out);
+
+/* ---- BLAS ---------------------------------------------------------------- */
+
+/* cuda::mp_dot<gridDim1, blockDim1, gridDim2, gridDim3, blockDim3>
+ * (src/blas/dot.cuh:84-108): r[0] = sum x_i * y_i.  The launch parameters are the
+ * reference's template arguments; gridDim3 and blockDim3 fix the summation order
+ * (gridDim3*blockDim3 strided partial sums, a tree over each block of
+ * blockDim3, then one block over the gridDim3 block sums), so results are
+ * bit-identical to the reference called with the same arguments.  `buffer`
+ * (len >= n in the reference) is accepted and not touched. */
+int mpres_dot(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *y, int incy, mp_array_t *r,
+              mp_array_t *buffer, int gridDim1, int blockDim1, int gridDim2, int gridDim3, int blockDim3,
+              void *stream);
+
+/* cuda::mp_gemv<gridDim1, blockDim1, gridDim2, blockDim3> (src/blas/gemv.cuh:150-269):
+ * y = alpha*op(A)*x + beta*y, A column-major.  blockDim3 fixes the summation order
+ * (blockDim3 strided partial sums per row, then a tree).  buffer1/buffer2 are
+ * accepted and not touched. */
+int mpres_gemv(int nmod, int trans, int m, int n, const mp_array_t *alpha, const mp_array_t *A, int lda,
+               const mp_array_t *x, int incx, const mp_array_t *beta, mp_array_t *y, int incy,
+               mp_array_t *buffer1, mp_array_t *buffer2, int gridDim1, int blockDim1, int gridDim2,
+               int blockDim3, void *stream);
+
+/* cuda::mp_gemm<blockDim1x, blockDim1y, gridDim2x, gridDim2y, blockDim3>
+ * (src/blas/gemm.cuh:69-168): C = alpha*A*B + beta*C, column-major, no-transpose
+ * only (the reference prints and returns for the other cases; this returns
+ * MPRES_ERR_NOT_SUPPORTED).  Launch parameters do not affect results. */
+int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_array_t *alpha,
+               const mp_array_t *A, int lda, const mp_array_t *B, int ldb, const mp_array_t *beta, mp_array_t *C,
+               int ldc, mp_array_t *buffer, int blockDim1x, int blockDim1y, int gridDim2x, int gridDim2y,
+               int blockDim3, void *stream);
+
+/* cuda::mp_spmv_csr<threads> (src/sparse/spmv/spmv_csr.cuh:48-63): y = A*x with a
+ * double CSR matrix and AoS mp_float_t vectors x (>= max(ja)+1) and y (>= m) in
+ * device memory.  The reference is a kernel its caller launches; `threads` is
+ * its template argument (any value gives the same result). */
+int mpres_spmv_csr(int nmod, int m, const csr_t *csr, const void *x, void *y, int threads, void *stream);
+
+/* cuda::mp_spmv_csrv<threads, threadsPerRow> (src/sparse/spmv/spmv_csrv.cuh:48-86);
+ * threadsPerRow in {1, 2, 4, 8, 16, 32} fixes the summation order. */
+int mpres_spmv_csrv(int nmod, int m, const csr_t *csr, const void *x, void *y, int threads, int threadsPerRow,
+                    void *stream);
+
+/* cuda::mp_spmv_ell<threads> (src/sparse/spmv/spmv_ell.cuh:49-67): ELLPACK,
+ * column-major slots, explicit zeros skipped. */
+int mpres_spmv_ell(int nmod, int m, int maxnzr, const ell_t *ell, const void *x, void *y, int threads,
+                   void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,52 @@
+/*
+ * Diagnostic entry points of libmpres_gb300.so (no counterpart in the
+ * reference, which has no benchmarking API).  They launch throughput
+ * microkernels on `stream` and return at once; the caller times them with
+ * events.  Each thread performs 8 independent chains of `iters` operations:
+ *   mpres_probe_mulmod: blocks*threads*iters*8 Barrett modular products
+ *                       (the residue reduction every RNS kernel uses);
+ *   mpres_probe_dadd:   blocks*threads*iters*8 directed-rounding double adds.
+ * `sink` is a device buffer of at least 8 bytes that the kernels may write.
+ */
+#ifndef MPRES_GB300_PROBE_H
+#define MPRES_GB300_PROBE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int mpres_probe_mulmod(int blocks, int threads, long long iters, void *sink, void *stream);
+int mpres_probe_dadd(int blocks, int threads, long long iters, void *sink, void *stream);
+
+/* out[i] = ceil(log2(x[i])) with the CUDA math library, the expression the
+ * reference's interval-evaluation refinement loop evaluates on the device
+ * (src/rns.cuh:848, :913); x and out are double[count] in device memory. */
+int mpres_probe_ceil_log2(const double *x, double *out, size_t count, void *stream);
+
+/* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
+ * element per thread: the device functions the BLAS kernels are built from,
+ * exposed so that each can be checked against the reference on its own.
+ *   MPRES_OP_ADD:   r[i] = x[i] + y[i]   cuda::mp_add (src/arith/add.cuh:190-202)
+ *   MPRES_OP_MUL:   r[i] = x[i] * y[i]   cuda::mp_mul (src/arith/mul.cuh:71-80)
+ *   MPRES_OP_MUL_D: r[i] = x[i] * d[i]   cuda::mp_mul_d (src/arith/muld.cuh:59-74), y = double[count] */
+#define MPRES_OP_ADD 0
+#define MPRES_OP_MUL 1
+#define MPRES_OP_MUL_D 2
+int mpres_elementwise(int nmod, int op, const void *x, const void *y, void *r, size_t count, void *stream);
+
+/* cuda::rns_scale2pow (src/rns.cuh:1132-1158): out = digits / 2^D[i], digits and out
+ * int[count * nmod] in device memory. */
+int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream);
+
+/* cuda::rns_eval_compute (fast = 0, src/rns.cuh:797-868) or rns_eval_compute_fast
+ * (fast = 1, :878-933): interval evaluation of digits[count * nmod] into low[count],
+ * upp[count] (er_float_t, device memory). */
+int mpres_rns_eval(int nmod, int fast, const int *digits, void *low, void *upp, size_t count, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,480 @@
+/*
+ * C ABI of libmpres_gb300.so (declared in include/mpres_gb300.h): argument
+ * checks with the reference's quick-return rules, constant set-up, containers,
+ * per-stream workspaces and the kernel launchers.
+ */
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/mpres_gb300.h"
+#include "../../include/mpres_gb300_probe.h"
+#include "kernels.h"
+#include "tables.h"
+
+namespace mpres {
+void host_set_d(const HostTables &t, const double *x, size_t count, void *out);
+}
+
+using namespace mpres;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+int ok() {
+    g_err.clear();
+    return MPRES_SUCCESS;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(MPRES_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+int set_slot(int nmod) { return nmod == 8 ? 0 : nmod == 16 ? 1 : nmod == 32 ? 2 : -1; }
+
+struct SetState {
+    bool host_ready = false;
+    HostTables host;
+    std::map<int, bool> device_ready; /* device ordinal -> uploaded */
+    std::map<int, std::pair<int *, int *>> device_tables;
+};
+
+std::mutex g_mu;
+SetState g_sets[3];
+
+struct WsKey {
+    int device;
+    cudaStream_t stream;
+    bool operator<(const WsKey &o) const { return device != o.device ? device < o.device : stream < o.stream; }
+};
+std::map<WsKey, Workspace> g_ws;
+
+template <int N> void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, Tables<N> &t) {
+    std::memset(&t, 0, sizeof(t));
+    for (int i = 0; i < N; i++) {
+        t.moduli[i] = h.moduli[i];
+        t.mu[i] = h.mu[i];
+        t.part_inv[i] = h.part_inv[i];
+        t.recip_rd[i] = h.recip_rd[i];
+        t.recip_ru[i] = h.recip_ru[i];
+        t.part_pow2_res30[i] = h.part_pow2_res[kScaleBits - 1][i];
+        for (int j = 0; j < N; j++) t.mrc_inv[i][j] = h.mrc_inv[i][j];
+    }
+    t.m_pow2_res30 = h.m_pow2_res[kScaleBits - 1];
+    t.eval_acc = h.eval_acc;
+    t.ref_factor = h.ref_factor;
+    t.mp_h = h.mp_h;
+    t.mp_j = h.mp_j;
+    t.mp_precision = h.mp_precision;
+    t.log2m = h.log2m;
+    t.unit_low = h.unit_low;
+    t.unit_upp = h.unit_upp;
+    t.inv_unit_low = h.inv_unit_low;
+    t.inv_unit_upp = h.inv_unit_upp;
+    t.pow2 = dpow2;
+    t.pow2_inv = dpow2_inv;
+}
+
+template <int N> cudaError_t upload_all(const HostTables &h, const int *dpow2, const int *dpow2_inv) {
+    Tables<N> t;
+    fill_tables<N>(h, dpow2, dpow2_inv, t);
+    cudaError_t e;
+    if ((e = upload_tables_dot(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_gemv(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_gemm(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_elementwise(N, &t)) != cudaSuccess) return e;
+    return upload_tables_spmv(N, &t);
+}
+
+/* requires g_mu held */
+int init_locked(int nmod) {
+    const int slot = set_slot(nmod);
+    if (slot < 0) return fail(MPRES_ERR_INVALID_VALUE, "unsupported moduli set size %d (8, 16 or 32)", nmod);
+    SetState &st = g_sets[slot];
+    if (!st.host_ready) {
+        if (!compute_host_tables(nmod, st.host)) return fail(MPRES_ERR_INVALID_VALUE, "tables of set %d", nmod);
+        st.host_ready = true;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (st.device_ready[dev]) return ok();
+    const HostTables &h = st.host;
+    const size_t pow2_bytes = sizeof(int) * (size_t)(h.log2m + 1) * nmod;
+    const size_t inv_bytes = sizeof(int) * (size_t)kScaleBits * nmod;
+    int *dpow2 = nullptr, *dinv = nullptr;
+    if ((e = cudaMalloc(&dpow2, pow2_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+    if ((e = cudaMalloc(&dinv, inv_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+    std::vector<int> inv((size_t)kScaleBits * nmod);
+    for (int r = 0; r < kScaleBits; r++)
+        for (int j = 0; j < nmod; j++) inv[(size_t)r * nmod + j] = h.pow2_inv[r][j];
+    if ((e = cudaMemcpy(dpow2, h.pow2, pow2_bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(tables)");
+    if ((e = cudaMemcpy(dinv, inv.data(), inv_bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(tables)");
+    if (nmod == 8) e = upload_all<8>(h, dpow2, dinv);
+    if (nmod == 16) e = upload_all<16>(h, dpow2, dinv);
+    if (nmod == 32) e = upload_all<32>(h, dpow2, dinv);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyToSymbol(tables)");
+    st.device_tables[dev] = {dpow2, dinv};
+    st.device_ready[dev] = true;
+    return ok();
+}
+
+int require(int nmod) {
+    const int slot = set_slot(nmod);
+    if (slot < 0) return fail(MPRES_ERR_INVALID_VALUE, "unsupported moduli set size %d (8, 16 or 32)", nmod);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_sets[slot].device_ready.find(dev);
+    if (it == g_sets[slot].device_ready.end() || !it->second)
+        return fail(MPRES_ERR_NOT_INITIALIZED, "mpres_init(%d) was not called on device %d", nmod, dev);
+    return MPRES_SUCCESS;
+}
+
+/* Workspace of (device, stream), grown on demand: the first call on a stream
+ * (or a call needing more room than before) allocates; later calls do not. */
+int workspace(cudaStream_t s, size_t bytes, Workspace &out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_mu);
+    Workspace &w = g_ws[WsKey{dev, s}];
+    if (w.bytes < bytes) {
+        if (w.ptr) {
+            cudaStreamSynchronize(s);
+            cudaFree(w.ptr);
+            w.ptr = nullptr;
+            w.bytes = 0;
+        }
+        size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
+        if ((e = cudaMalloc(&w.ptr, want)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(workspace)");
+        w.bytes = want;
+    }
+    out = w;
+    return MPRES_SUCCESS;
+}
+
+size_t mp_size(int nmod) { return 4 * (size_t)nmod + 40; }
+
+} // namespace
+
+extern "C" {
+
+const char *mpres_last_error(void) { return g_err.c_str(); }
+
+size_t mpres_mp_float_size(int nmod) { return set_slot(nmod) < 0 ? 0 : mp_size(nmod); }
+
+int mpres_init(int nmod) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return init_locked(nmod);
+}
+
+int mpres_get_int_constants(int nmod, int *out) {
+    const int slot = set_slot(nmod);
+    if (slot < 0 || !out) return fail(MPRES_ERR_INVALID_VALUE, "unsupported moduli set size %d", nmod);
+    std::lock_guard<std::mutex> lk(g_mu);
+    SetState &st = g_sets[slot];
+    if (!st.host_ready) {
+        if (!compute_host_tables(nmod, st.host)) return fail(MPRES_ERR_INVALID_VALUE, "tables of set %d", nmod);
+        st.host_ready = true;
+    }
+    out[0] = st.host.mp_precision;
+    out[1] = st.host.mp_h;
+    out[2] = st.host.mp_j;
+    out[3] = st.host.ref_factor;
+    out[4] = st.host.log2m;
+    return ok();
+}
+
+int mpres_array_init(int nmod, mp_array_t *a, size_t size) {
+    if (!a || set_slot(nmod) < 0) return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_init: bad arguments");
+    std::memset(a, 0, sizeof(*a));
+    const size_t n = size ? size : 1;
+    cudaError_t e;
+    if ((e = cudaMalloc(&a->digits, sizeof(int) * (size_t)nmod * n)) != cudaSuccess ||
+        (e = cudaMalloc(&a->sign, sizeof(int) * n)) != cudaSuccess ||
+        (e = cudaMalloc(&a->exp, sizeof(int) * n)) != cudaSuccess ||
+        (e = cudaMalloc(&a->eval, sizeof(er_float_t) * 2 * n)) != cudaSuccess ||
+        (e = cudaMalloc(&a->buf, sizeof(mpres_int4) * n)) != cudaSuccess ||
+        (e = cudaMalloc(&a->len, sizeof(int))) != cudaSuccess)
+        return cuda_fail(e, "mpres_array_init");
+    int len = (int)size;
+    if ((e = cudaMemcpy(a->len, &len, sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "mpres_array_init");
+    return ok();
+}
+
+int mpres_array_clear(mp_array_t *a) {
+    if (!a) return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_clear: null array");
+    cudaFree(a->digits);
+    cudaFree(a->sign);
+    cudaFree(a->exp);
+    cudaFree(a->eval);
+    cudaFree(a->buf);
+    cudaFree(a->len);
+    std::memset(a, 0, sizeof(*a));
+    cudaError_t e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_array_clear");
+}
+
+int mpres_array_host2device(int nmod, mp_array_t *dst, const void *host_src, size_t size) {
+    if (!dst || (!host_src && size) || set_slot(nmod) < 0)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_host2device: bad arguments");
+    if (size == 0) return ok();
+    const size_t sz = mp_size(nmod);
+    std::vector<int> digits((size_t)nmod * size), sign(size), exp(size);
+    std::vector<er_float_t> eval(2 * size);
+    const char *src = static_cast<const char *>(host_src);
+    for (size_t i = 0; i < size; i++) {
+        const char *p = src + i * sz;
+        std::memcpy(&digits[i * nmod], p, 4 * (size_t)nmod);
+        std::memcpy(&sign[i], p + 4 * nmod, 4);
+        std::memcpy(&exp[i], p + 4 * nmod + 4, 4);
+        std::memcpy(&eval[i], p + 4 * nmod + 8, 16);
+        std::memcpy(&eval[size + i], p + 4 * nmod + 24, 16);
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpy(dst->digits, digits.data(), 4 * digits.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(dst->sign, sign.data(), 4 * size, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(dst->exp, exp.data(), 4 * size, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(dst->eval, eval.data(), sizeof(er_float_t) * 2 * size, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "mpres_array_host2device");
+    return ok();
+}
+
+int mpres_array_device2host(int nmod, void *host_dst, const mp_array_t *src, size_t size) {
+    if (!src || (!host_dst && size) || set_slot(nmod) < 0)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_device2host: bad arguments");
+    if (size == 0) return ok();
+    const size_t sz = mp_size(nmod);
+    std::vector<int> digits((size_t)nmod * size), sign(size), exp(size);
+    std::vector<er_float_t> eval(2 * size);
+    cudaError_t e;
+    if ((e = cudaMemcpy(digits.data(), src->digits, 4 * digits.size(), cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (e = cudaMemcpy(sign.data(), src->sign, 4 * size, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (e = cudaMemcpy(exp.data(), src->exp, 4 * size, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (e = cudaMemcpy(eval.data(), src->eval, sizeof(er_float_t) * 2 * size, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "mpres_array_device2host");
+    char *dst = static_cast<char *>(host_dst);
+    for (size_t i = 0; i < size; i++) {
+        char *p = dst + i * sz;
+        std::memcpy(p, &digits[i * nmod], 4 * (size_t)nmod);
+        std::memcpy(p + 4 * nmod, &sign[i], 4);
+        std::memcpy(p + 4 * nmod + 4, &exp[i], 4);
+        std::memcpy(p + 4 * nmod + 8, &eval[i], 16);
+        std::memcpy(p + 4 * nmod + 24, &eval[size + i], 16);
+    }
+    return ok();
+}
+
+int mpres_csr_init(csr_t *csr, int m, int nnz) {
+    if (!csr || m < 0 || nnz < 0) return fail(MPRES_ERR_INVALID_VALUE, "mpres_csr_init: bad arguments");
+    cudaError_t e;
+    if ((e = cudaMalloc(&csr->as, sizeof(double) * (size_t)(nnz ? nnz : 1))) != cudaSuccess ||
+        (e = cudaMalloc(&csr->ja, sizeof(int) * (size_t)(nnz ? nnz : 1))) != cudaSuccess ||
+        (e = cudaMalloc(&csr->irp, sizeof(int) * (size_t)(m + 1))) != cudaSuccess)
+        return cuda_fail(e, "mpres_csr_init");
+    return ok();
+}
+
+int mpres_csr_host2device(csr_t *dev, const csr_t *host, int m, int nnz) {
+    if (!dev || !host || m < 0 || nnz < 0) return fail(MPRES_ERR_INVALID_VALUE, "mpres_csr_host2device: bad arguments");
+    cudaError_t e;
+    if ((nnz && (e = cudaMemcpy(dev->as, host->as, sizeof(double) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (nnz && (e = cudaMemcpy(dev->ja, host->ja, sizeof(int) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess) ||
+        (e = cudaMemcpy(dev->irp, host->irp, sizeof(int) * (size_t)(m + 1), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "mpres_csr_host2device");
+    return ok();
+}
+
+int mpres_csr_clear(csr_t *csr) {
+    if (!csr) return fail(MPRES_ERR_INVALID_VALUE, "mpres_csr_clear: null");
+    cudaFree(csr->as);
+    cudaFree(csr->ja);
+    cudaFree(csr->irp);
+    std::memset(csr, 0, sizeof(*csr));
+    cudaError_t e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_csr_clear");
+}
+
+int mpres_ell_init(ell_t *ell, int m, int maxnzr) {
+    if (!ell || m < 0 || maxnzr < 0) return fail(MPRES_ERR_INVALID_VALUE, "mpres_ell_init: bad arguments");
+    size_t slots = (size_t)m * maxnzr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&ell->as, sizeof(double) * (slots ? slots : 1))) != cudaSuccess ||
+        (e = cudaMalloc(&ell->ja, sizeof(int) * (slots ? slots : 1))) != cudaSuccess)
+        return cuda_fail(e, "mpres_ell_init");
+    return ok();
+}
+
+int mpres_ell_host2device(ell_t *dev, const ell_t *host, int m, int maxnzr) {
+    if (!dev || !host || m < 0 || maxnzr < 0)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_ell_host2device: bad arguments");
+    size_t slots = (size_t)m * maxnzr;
+    cudaError_t e;
+    if (slots && ((e = cudaMemcpy(dev->as, host->as, sizeof(double) * slots, cudaMemcpyHostToDevice)) != cudaSuccess ||
+                  (e = cudaMemcpy(dev->ja, host->ja, sizeof(int) * slots, cudaMemcpyHostToDevice)) != cudaSuccess))
+        return cuda_fail(e, "mpres_ell_host2device");
+    return ok();
+}
+
+int mpres_ell_clear(ell_t *ell) {
+    if (!ell) return fail(MPRES_ERR_INVALID_VALUE, "mpres_ell_clear: null");
+    cudaFree(ell->as);
+    cudaFree(ell->ja);
+    std::memset(ell, 0, sizeof(*ell));
+    cudaError_t e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_ell_clear");
+}
+
+int mpres_set_d(int nmod, const double *x, size_t count, void *out) {
+    const int slot = set_slot(nmod);
+    if (slot < 0 || (count && (!x || !out))) return fail(MPRES_ERR_INVALID_VALUE, "mpres_set_d: bad arguments");
+    const HostTables *t;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        SetState &st = g_sets[slot];
+        if (!st.host_ready) {
+            if (!compute_host_tables(nmod, st.host)) return fail(MPRES_ERR_INVALID_VALUE, "tables of set %d", nmod);
+            st.host_ready = true;
+        }
+        t = &st.host;
+    }
+    host_set_d(*t, x, count, out);
+    return ok();
+}
+
+int mpres_dot(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *y, int incy, mp_array_t *r,
+              mp_array_t *buffer, int gridDim1, int blockDim1, int gridDim2, int gridDim3, int blockDim3,
+              void *stream) {
+    (void)buffer; (void)gridDim1; (void)blockDim1; (void)gridDim2;
+    if (int st = require(nmod)) return st;
+    if (n <= 0) return ok(); /* src/blas/dot.cuh:88-90 */
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dot: null array");
+    if (gridDim3 <= 0 || blockDim3 <= 0 || blockDim3 > 1024)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_dot: gridDim3 %d / blockDim3 %d out of range", gridDim3, blockDim3);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, (size_t)gridDim3 * mp_size(nmod), ws)) return st;
+    cudaError_t e = launch_dot(nmod, n, *x, incx, *y, incy, *r, gridDim3, blockDim3, ws, s);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_dot");
+}
+
+int mpres_gemv(int nmod, int trans, int m, int n, const mp_array_t *alpha, const mp_array_t *A, int lda,
+               const mp_array_t *x, int incx, const mp_array_t *beta, mp_array_t *y, int incy, mp_array_t *buffer1,
+               mp_array_t *buffer2, int gridDim1, int blockDim1, int gridDim2, int blockDim3, void *stream) {
+    (void)buffer1; (void)buffer2; (void)gridDim1; (void)blockDim1; (void)gridDim2;
+    if (int st = require(nmod)) return st;
+    /* src/blas/gemv.cuh:155-161 */
+    if (m <= 0 || n <= 0) return ok();
+    if (incx == 0 || incy == 0 || lda < (m > 1 ? m : 1)) return ok();
+    if (!alpha || !A || !x || !beta || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_gemv: null array");
+    if (blockDim3 <= 0 || blockDim3 > 1024)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_gemv: blockDim3 %d out of range", blockDim3);
+    const bool tr = (trans != MPRES_NO_TRANS);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, (size_t)(tr ? m : n) * mp_size(nmod), ws)) return st;
+    cudaError_t e = launch_gemv(nmod, tr, m, n, *alpha, *A, lda, *x, incx, *beta, *y, incy, blockDim3, ws, s);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemv");
+}
+
+int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_array_t *alpha, const mp_array_t *A,
+               int lda, const mp_array_t *B, int ldb, const mp_array_t *beta, mp_array_t *C, int ldc,
+               mp_array_t *buffer, int blockDim1x, int blockDim1y, int gridDim2x, int gridDim2y, int blockDim3,
+               void *stream) {
+    (void)buffer; (void)blockDim1x; (void)blockDim1y; (void)gridDim2x; (void)gridDim2y; (void)blockDim3;
+    if (int st = require(nmod)) return st;
+    /* src/blas/gemm.cuh:77-96 */
+    if (m <= 0 || n <= 0 || k <= 0) return ok();
+    if (transa == MPRES_NO_TRANS && lda < (m > 1 ? m : 1)) return ok();
+    if (transa == MPRES_TRANS && lda < (k > 1 ? k : 1)) return ok();
+    if (transb == MPRES_NO_TRANS && ldb < (k > 1 ? k : 1)) return ok();
+    if (transb == MPRES_TRANS && ldb < (n > 1 ? n : 1)) return ok();
+    if (ldc < (m > 1 ? m : 1)) return ok();
+    if (transa != MPRES_NO_TRANS || transb != MPRES_NO_TRANS)
+        return fail(MPRES_ERR_NOT_SUPPORTED, "mpres_gemm: only non-transposed matrices are supported");
+    if (!alpha || !A || !B || !beta || !C) return fail(MPRES_ERR_INVALID_VALUE, "mpres_gemm: null array");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, s);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemm");
+}
+
+int mpres_spmv_csr(int nmod, int m, const csr_t *csr, const void *x, void *y, int threads, void *stream) {
+    (void)threads;
+    if (int st = require(nmod)) return st;
+    if (m <= 0) return ok();
+    if (!csr || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_csr: null argument");
+    cudaError_t e = launch_spmv_csr(nmod, m, *csr, x, y, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_csr");
+}
+
+int mpres_spmv_csrv(int nmod, int m, const csr_t *csr, const void *x, void *y, int threads, int threadsPerRow,
+                    void *stream) {
+    (void)threads;
+    if (int st = require(nmod)) return st;
+    if (threadsPerRow < 1 || threadsPerRow > 32 || (threadsPerRow & (threadsPerRow - 1)))
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_csrv: threadsPerRow %d not a power of two <= 32",
+                    threadsPerRow);
+    if (m <= 0) return ok();
+    if (!csr || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_csrv: null argument");
+    cudaError_t e = launch_spmv_csrv(nmod, m, threadsPerRow, *csr, x, y, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_csrv");
+}
+
+int mpres_spmv_ell(int nmod, int m, int maxnzr, const ell_t *ell, const void *x, void *y, int threads,
+                   void *stream) {
+    (void)threads;
+    if (int st = require(nmod)) return st;
+    if (m <= 0) return ok();
+    if (maxnzr < 0 || !ell || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_ell: bad argument");
+    cudaError_t e = launch_spmv_ell(nmod, m, maxnzr, *ell, x, y, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_ell");
+}
+
+int mpres_elementwise(int nmod, int op, const void *x, const void *y, void *r, size_t count, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (op != MPRES_OP_ADD && op != MPRES_OP_MUL && op != MPRES_OP_MUL_D)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_elementwise: unknown op %d", op);
+    if (count == 0) return ok();
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_elementwise: null pointer");
+    cudaError_t e = launch_elementwise(nmod, op, x, y, r, (long long)count, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_elementwise");
+}
+
+int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count == 0) return ok();
+    if (!digits || !D || !out) return fail(MPRES_ERR_INVALID_VALUE, "mpres_rns_scale2pow: null pointer");
+    cudaError_t e = launch_scale2pow(nmod, digits, D, out, (long long)count, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_rns_scale2pow");
+}
+
+int mpres_rns_eval(int nmod, int fast, const int *digits, void *low, void *upp, size_t count, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count == 0) return ok();
+    if (!digits || !low || !upp) return fail(MPRES_ERR_INVALID_VALUE, "mpres_rns_eval: null pointer");
+    cudaError_t e = launch_eval(nmod, fast, digits, static_cast<er_t *>(low), static_cast<er_t *>(upp),
+                                (long long)count, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_rns_eval");
+}
+
+} // extern "C"

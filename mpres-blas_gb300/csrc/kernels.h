@@ -1,0 +1,52 @@
+/*
+ * Host-side launchers of the kernels (one translation unit per operation) and
+ * the per-unit table upload hooks.  Internal to libmpres_gb300.so.
+ */
+#ifndef MPRES_KERNELS_H
+#define MPRES_KERNELS_H
+
+#include <cuda_runtime.h>
+
+#include "../../include/mpres_gb300.h"
+#include "tables.h"
+
+namespace mpres {
+
+cudaError_t upload_tables_dot(int n, const void *tab);
+cudaError_t upload_tables_gemv(int n, const void *tab);
+cudaError_t upload_tables_gemm(int n, const void *tab);
+cudaError_t upload_tables_spmv(int n, const void *tab);
+cudaError_t upload_tables_elementwise(int n, const void *tab);
+
+/* Scratch for one call, carved from a per-device workspace. */
+struct Workspace {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+/* mp_dot: g3 block sums go to ws (g3 * (4n+40) bytes). */
+cudaError_t launch_dot(int nmod, int n, const mp_array_t &x, int incx, const mp_array_t &y, int incy,
+                       const mp_array_t &r, int g3, int b3, Workspace ws, cudaStream_t s);
+
+cudaError_t launch_gemv(int nmod, bool trans, int m, int n, const mp_array_t &alpha, const mp_array_t &A, int lda,
+                        const mp_array_t &x, int incx, const mp_array_t &beta, const mp_array_t &y, int incy,
+                        int b3, Workspace ws, cudaStream_t s);
+
+cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
+                        const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
+                        cudaStream_t s);
+
+cudaError_t launch_spmv_csr(int nmod, int m, const csr_t &csr, const void *x, void *y, cudaStream_t s);
+cudaError_t launch_spmv_csrv(int nmod, int m, int tpr, const csr_t &csr, const void *x, void *y, cudaStream_t s);
+cudaError_t launch_spmv_ell(int nmod, int m, int maxnzr, const ell_t &ell, const void *x, void *y, cudaStream_t s);
+
+cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, void *r, long long count,
+                               cudaStream_t s);
+cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,
+                             cudaStream_t s);
+cudaError_t launch_eval(int nmod, int fast, const int *digits, er_t *low, er_t *upp, long long count,
+                        cudaStream_t s);
+
+} // namespace mpres
+
+#endif

@@ -1,0 +1,568 @@
+/*
+ * Device arithmetic of RNS multiple-precision numbers, one number per thread.
+ *
+ * Semantics are those of the reference's device code (namespace cuda of
+ * src/modular.cuh, src/extrange.cuh, src/pairwise.cuh, src/rns.cuh and
+ * src/arith/{arith_utils,add,mul,muld}.cuh), bit for bit: same residues, sign,
+ * exponent and interval evaluation.  The implementation is this library's own:
+ *  - residues are reduced with a 32-bit Barrett step (one IMAD.WIDE, one
+ *    IMAD.HI, one IMAD and two min-subtractions) instead of 64-bit `%`;
+ *  - multiplications of doubles by 0/1/-1 factors, the exponent/significand
+ *    splits and the zero tests are bit operations on the integer pipes, and
+ *    give exactly the double the reference's multiplications give;
+ *  - the directed-rounding operations the interval bounds need (the
+ *    __dadd_rd/__dmul_ru/__ddiv_rd... intrinsics) are kept: they are IEEE
+ *    correctly rounded, so any exact method gives the same bits;
+ *  - pairwise sums evaluate the reference's tree depth first, computing leaves
+ *    on demand, so register use stays logarithmic in the set size.
+ *
+ * The number of moduli N is a template parameter; each translation unit that
+ * includes this header owns a __constant__ copy of the tables of N = 8, 16, 32
+ * (MPRES_DEFINE_TABLES), uploaded by mpres_init().
+ */
+#ifndef MPRES_MP_DEVICE_CUH
+#define MPRES_MP_DEVICE_CUH
+
+#include <cstdint>
+
+#include "tables.h"
+
+namespace mpres {
+
+template <int N>
+struct mp_t {
+    int d[N];
+    int sign;
+    int exp;
+    er_t ev[2];
+};
+
+namespace dev {
+
+constexpr uint64_t kSign = 1ull << 63;
+constexpr uint64_t kZeroExpMask = ((1ull << 52) - 1) | kSign;
+constexpr uint64_t kBiasExpMask = 1023ull << 52;
+
+template <int N> __device__ __forceinline__ const Tables<N> &T();
+
+__device__ __forceinline__ uint64_t dbits(double d) { return (uint64_t)__double_as_longlong(d); }
+__device__ __forceinline__ double bdbl(uint64_t u) { return __longlong_as_double((long long)u); }
+/* x != 0 for a double (false for +0 and -0) */
+__device__ __forceinline__ bool dnz(double d) { return (dbits(d) << 1) != 0; }
+/* x < 0 for a non-NaN double */
+__device__ __forceinline__ bool dneg(double d) { return (dbits(d) >> 63) && dnz(d); }
+/* x * f for f in {-1, 0, 1}: exactly the IEEE product, computed on bits */
+__device__ __forceinline__ double dscale_sign(double x, int f) {
+    uint64_t u = dbits(x);
+    if (f == 0) return bdbl(u & kSign);
+    return f < 0 ? bdbl(u ^ kSign) : x;
+}
+
+template <bool UP> __device__ __forceinline__ double dadd(double a, double b) {
+    return UP ? __dadd_ru(a, b) : __dadd_rd(a, b);
+}
+template <bool UP> __device__ __forceinline__ double dsub(double a, double b) {
+    return UP ? __dsub_ru(a, b) : __dsub_rd(a, b);
+}
+template <bool UP> __device__ __forceinline__ double dmul(double a, double b) {
+    return UP ? __dmul_ru(a, b) : __dmul_rd(a, b);
+}
+template <bool UP> __device__ __forceinline__ double ddiv(double a, double b) {
+    return UP ? __ddiv_ru(a, b) : __ddiv_rd(a, b);
+}
+
+/* ---------------------------- residues ---------------------------------- */
+
+/* x*y mod m for 0 <= x, y < 2^31, 2^30 < m < 2^32/3, mu = floor(2^62/m):
+ * the Barrett quotient is at most 2 short, so r < 3m < 2^32. */
+__device__ __forceinline__ uint32_t mulmod(uint32_t x, uint32_t y, uint32_t m, uint32_t mu) {
+    uint64_t p = (uint64_t)x * y;
+    uint32_t q = __umulhi((uint32_t)(p >> 30), mu);
+    uint32_t r = (uint32_t)p - q * m;
+    r = min(r, r - m);
+    r = min(r, r - m);
+    return r;
+}
+/* a mod m for 0 <= a < 2m */
+__device__ __forceinline__ uint32_t reduce2(uint32_t a, uint32_t m) { return min(a, a - m); }
+
+template <int N> __device__ __forceinline__ int mulmod_i(int x, int y, int i) {
+    const Tables<N> &t = T<N>();
+    return (int)mulmod((uint32_t)x, (uint32_t)y, (uint32_t)t.moduli[i], t.mu[i]);
+}
+
+/* ------------------------ extended-range floats ------------------------- */
+
+/* er_adjust, src/extrange.cuh:412-421 */
+__device__ __forceinline__ void er_adjust(er_t &x) {
+    uint64_t u = dbits(x.frac);
+    bool nz = (u << 1) != 0;
+    long long e = (long long)((uint64_t)x.exp + ((u & ~kSign) >> 52) - 1023ull);
+    x.exp = nz ? e : 0;
+    x.frac = nz ? bdbl((u & kZeroExpMask) | kBiasExpMask) : bdbl(u & kSign);
+}
+
+/* er_set_d, src/extrange.cuh:93-107 */
+__device__ __forceinline__ void er_set_d(er_t &r, double x) {
+    uint64_t u = dbits(x);
+    if (dnz(x)) {
+        r.exp = (long long)((u & ~kSign) >> 52) - 1023;
+        r.frac = bdbl((u & kZeroExpMask) | kBiasExpMask);
+    } else {
+        r.exp = 0;
+        r.frac = 0.0;
+    }
+}
+
+/* er_add_rd / er_add_ru, src/extrange.cuh:451-490 */
+template <bool UP> __device__ __forceinline__ er_t er_add(er_t x, er_t y) {
+    const bool xnz = dnz(x.frac), ynz = dnz(y.frac);
+    if (!xnz) x.exp = 0;
+    if (!ynz) y.exp = 0;
+    const long long dexp = (xnz && ynz) ? x.exp - y.exp : 0;
+    er_t r;
+    if (dexp > 0) {
+        r.exp = x.exp;
+        r.frac = dadd<UP>(x.frac, scalbn(y.frac, (int)-dexp));
+    } else if (dexp < 0) {
+        r.exp = y.exp;
+        r.frac = dadd<UP>(y.frac, scalbn(x.frac, (int)dexp));
+    } else {
+        r.exp = (x.exp == 0) ? y.exp : x.exp;
+        r.frac = dadd<UP>(x.frac, y.frac);
+    }
+    er_adjust(r);
+    return r;
+}
+
+/* er_md_rd / er_md_ru (x*y/z), src/extrange.cuh:627-644 */
+template <bool UP> __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z) {
+    er_t r;
+    r.exp = x.exp + y.exp - z.exp;
+    r.frac = ddiv<UP>(dmul<UP>(x.frac, y.frac), z.frac);
+    er_adjust(r);
+    return r;
+}
+
+/* ---------------------------- pairwise sums ------------------------------ */
+
+/* The balanced tree of src/pairwise.cuh:855-929 over a power-of-two SPAN with
+ * LEN real leaves (missing leaves read 0); leaf(i) is evaluated on demand. */
+template <int SPAN, int LEN, bool UP, class F>
+__device__ __forceinline__ double psum_node(const F &leaf, int base) {
+    if constexpr (SPAN == 2) {
+        return dadd<UP>(leaf(base), LEN > 1 ? leaf(base + 1) : 0.0);
+    } else {
+        double s1 = psum_node<SPAN / 2, LEN, UP>(leaf, base);
+        double s2 = 0.0;
+        if constexpr (LEN > SPAN / 2) s2 = psum_node<SPAN / 2, LEN - SPAN / 2, UP>(leaf, base + SPAN / 2);
+        return dadd<UP>(s1, s2);
+    }
+}
+__host__ __device__ constexpr int psum_span(int len) {
+    int s = 8;
+    while (s <= len) s *= 2;
+    return s;
+}
+template <int N, bool UP, class F> __device__ __forceinline__ double psum(const F &leaf) {
+    static_assert(N >= 4, "moduli sets have at least 4 moduli");
+    return psum_node<psum_span(N), N, UP>(leaf, 0);
+}
+
+/* --------------------------- RNS algorithms ------------------------------ */
+
+/* Most significant mixed-radix digit, src/rns.cuh:587-603 (cuda::mrd).  Rare
+ * path (ambiguous interval evaluations): kept out of line. */
+template <int N> __device__ __noinline__ int mrd(const int *x) {
+    const Tables<N> &t = T<N>();
+    int mixed[N];
+    for (int i = 0; i < N; i++) {
+        int v = x[i];
+        const uint32_t m = (uint32_t)t.moduli[i];
+        for (int j = 0; j < i; j++) {
+            if (v < mixed[j]) v = (int)reduce2((uint32_t)v - (uint32_t)mixed[j] + m, m);
+            else v = v - mixed[j];
+            v = (int)mulmod((uint32_t)v, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
+        }
+        mixed[i] = v;
+    }
+    return mixed[N - 1];
+}
+
+/* mrc_compare_rns, src/rns.cuh:570-630 (rare path) */
+template <int N> __device__ __noinline__ int mrc_compare(const int *x, const int *y) {
+    const Tables<N> &t = T<N>();
+    int mx[N], my[N];
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i];
+        int vx = x[i], vy = y[i];
+        for (int j = 0; j < i; j++) {
+            vx = (vx < mx[j]) ? (int)reduce2((uint32_t)vx - (uint32_t)mx[j] + m, m) : vx - mx[j];
+            vx = (int)mulmod((uint32_t)vx, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
+            vy = (vy < my[j]) ? (int)reduce2((uint32_t)vy - (uint32_t)my[j] + m, m) : vy - my[j];
+            vy = (int)mulmod((uint32_t)vy, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
+        }
+        mx[i] = vx;
+        my[i] = vy;
+    }
+    for (int i = N - 1; i >= 0; i--) {
+        if (mx[i] > my[i]) return 1;
+        if (my[i] > mx[i]) return -1;
+    }
+    return 0;
+}
+
+template <int N> __device__ __forceinline__ int pow2_row_index(int r) {
+    /* out-of-table rows only occur for an operand whose digits are all zero,
+     * where any row gives the same product (the reference reads past the end) */
+    return r > T<N>().log2m ? T<N>().log2m : r;
+}
+
+/* Refinement loop of rns_eval_compute[_fast], src/rns.cuh:843-867 / :908-932 */
+template <int N>
+__device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &upp) {
+    const Tables<N> &t = T<N>();
+    int K = 0;
+    for (int guard = 0; sumu < t.eval_acc && guard < 4096; guard++) {
+        double a = -(ceil(log2(sumu)) + 1);
+        int k = (int)(a > t.ref_factor ? a : (double)t.ref_factor);
+        k = pow2_row_index<N>(k < 0 ? 0 : k);
+        const int *row = t.pow2 + (size_t)k * N;
+#pragma unroll
+        for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
+        sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+        sumu = __dsub_ru(sumu, (double)(unsigned int)sumu);
+        K += k;
+    }
+    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
+    suml = __dsub_rd(suml, (double)(unsigned int)suml);
+    er_set_d(low, suml);
+    er_set_d(upp, sumu);
+    low.exp -= K;
+    upp.exp -= K;
+}
+
+/* cuda::rns_eval_compute_fast, src/rns.cuh:878-933 */
+template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp, const int *x) {
+    const Tables<N> &t = T<N>();
+    int s[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
+    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
+    double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+    if (!dnz(suml) && !dnz(sumu)) {
+        low.frac = 0.0; low.exp = 0;
+        upp.frac = 0.0; upp.exp = 0;
+        return;
+    }
+    suml = __dsub_rd(suml, (double)(unsigned int)suml);
+    sumu = __dsub_ru(sumu, (double)(unsigned int)sumu);
+    if (sumu >= t.eval_acc) {
+        er_set_d(low, suml);
+        er_set_d(upp, sumu);
+        return;
+    }
+    eval_refine<N>(s, sumu, low, upp);
+}
+
+/* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */
+template <int N> __device__ __forceinline__ int rank_full(const int *x, const int *s) {
+    const Tables<N> &t = T<N>();
+    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
+    double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+    unsigned int whl = (unsigned int)suml, whu = (unsigned int)sumu;
+    if (whl == whu) return (int)whl;
+    return (mrd<N>(x) == 0) ? (int)whu : (int)whl;
+}
+/* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096 */
+template <int N> __device__ __forceinline__ int rank_fast(const int *s) {
+    const Tables<N> &t = T<N>();
+    return (int)psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+}
+
+/* cuda::make_scaling_step, src/rns.cuh:1101-1124, for 1 <= j <= 30.  Residues
+ * modulo 2^j are low bits, so the sum runs in wrapping 32-bit arithmetic. */
+template <int N>
+__device__ __forceinline__ void scaling_step(int *y, int k, int j, const int *x, const int *c) {
+    const Tables<N> &t = T<N>();
+    const uint32_t mask = (j >= 32) ? 0xffffffffu : ((1u << j) - 1);
+    uint32_t residue = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) residue += ((uint32_t)t.part_pow2_res30[i] & mask) * (uint32_t)c[i];
+    residue -= (uint32_t)k * ((uint32_t)t.m_pow2_res30 & mask);
+    residue &= mask;
+    const int *inv = t.pow2_inv + (size_t)(j - 1) * N;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i];
+        /* residue < 2^30 < m, so residue mod m_i is residue */
+        uint32_t multiple = reduce2((uint32_t)x[i] - residue + m, m);
+        y[i] = (int)mulmod(multiple, (uint32_t)__ldg(inv + i), m, t.mu[i]);
+    }
+}
+
+/* cuda::rns_scale2pow, src/rns.cuh:1132-1158; in place */
+template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int D) {
+    const Tables<N> &t = T<N>();
+    int c[N];
+    int steps = (int)(D / kScaleBits);
+    if (steps > 0) {
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
+        int k = rank_full<N>(x, c);
+        scaling_step<N>(x, k, kScaleBits, x, c);
+        steps -= 1;
+    }
+    for (; steps > 0; steps--) {
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
+        int k = rank_fast<N>(c);
+        scaling_step<N>(x, k, kScaleBits, x, c);
+    }
+    unsigned int d = D % kScaleBits;
+    if (d > 0) {
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
+        int k = (d < D) ? rank_full<N>(x, c) : rank_fast<N>(c);
+        scaling_step<N>(x, k, (int)d, x, c);
+    }
+}
+
+/* Rounding after an operation: src/arith/arith_utils.cuh:172-190 (mp_round with
+ * mp_get_rnd_bits), also mp_vector_round_kernel (src/mpvector.cuh:669-688) and
+ * mp_matrix_round_kernel (src/mpmatrix.cuh:410-428). */
+template <int N> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
+    r.exp += bits;
+    scale2pow<N>(r.d, (unsigned int)bits);
+    eval_fast<N>(r.ev[0], r.ev[1], r.d);
+}
+template <int N> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
+    if (dnz(r.ev[1].frac) && r.ev[1].exp >= T<N>().mp_h) {
+        int bits = (int)(r.ev[1].exp - T<N>().mp_h + 1);
+        if (bits > 0) round_slow<N>(r, bits);
+    }
+}
+
+/* cuda::sign_estimate, src/arith/arith_utils.cuh:197-206 (rare path) */
+template <int N>
+__device__ __noinline__ int sign_estimate(const int *dx, const int *dy, int sx, int sy, int gamma, int theta, int nzx,
+                                          int nzy) {
+    const Tables<N> &t = T<N>();
+    int lx[N], ly[N];
+    const int *pg = t.pow2 + (size_t)pow2_row_index<N>(gamma) * N;
+    const int *pt = t.pow2 + (size_t)pow2_row_index<N>(theta) * N;
+    for (int i = 0; i < N; i++) {
+        lx[i] = nzx * mulmod_i<N>(dx[i], __ldg(pg + i), i);
+        ly[i] = nzy * mulmod_i<N>(dy[i], __ldg(pt + i), i);
+    }
+    int cmp = mrc_compare<N>(lx, ly);
+    return (cmp < 0 ? sy : sx) * (cmp != 0);
+}
+
+/* ------------------------ multiple-precision ops ------------------------- */
+
+template <int N> __device__ __forceinline__ void set_zero(mp_t<N> &z) {
+#pragma unroll
+    for (int i = 0; i < N; i++) z.d[i] = 0;
+    z.sign = 0;
+    z.exp = 0;
+    z.ev[0].frac = 0.0; z.ev[0].exp = 0;
+    z.ev[1].frac = 0.0; z.ev[1].exp = 0;
+}
+
+/* cuda::mp_add: mp_add_common (src/arith/add.cuh:126-188) and the rounding of
+ * its overloads (:190-271). */
+template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y) {
+    const Tables<N> &t = T<N>();
+    int ex = x.exp, ey = y.exp, sx = x.sign, sy = y.sign;
+    const int dexp = ex - ey;
+    int gamma = dexp > 0 ? dexp : 0;
+    int theta = dexp < 0 ? -dexp : 0;
+    const int nzx = (!dnz(y.ev[1].frac) || (theta + y.ev[1].exp) < t.mp_j);
+    const int nzy = (!dnz(x.ev[1].frac) || (gamma + x.ev[1].exp) < t.mp_j);
+    gamma *= nzy;
+    theta *= nzx;
+    ex = (ex - gamma) * nzx;
+    ey = (ey - theta) * nzy;
+    sx *= nzx;
+    sy *= nzy;
+    const int fx = (1 - 2 * sx) * nzx;
+    const int fy = (1 - 2 * sy) * nzy;
+    er_t ax[2], ay[2];
+    ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
+    ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
+    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
+    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
+    er_t ev[2];
+    ev[0] = er_add<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
+    ev[1] = er_add<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
+    int sign = dneg(ev[0].frac);
+    if (sign != (int)dneg(ev[1].frac)) {
+        sign = sign_estimate<N>(x.d, y.d, sx, sy, gamma, theta, nzx, nzy);
+        er_t u = t.unit_low;
+        if (sign) u.frac = -u.frac;
+        ev[sign] = u;
+    }
+    r.sign = sign;
+    r.exp = (ex == 0) ? ey : ex;
+    /* cuda::rns_axby_cd, src/modular.cuh:306-314: (2^gamma*x*fx + 2^theta*y*fy) mod m */
+    const int *pg = t.pow2 + (size_t)pow2_row_index<N>(gamma) * N;
+    const int *pt = t.pow2 + (size_t)pow2_row_index<N>(theta) * N;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i];
+        uint32_t u = gamma ? mulmod((uint32_t)__ldg(pg + i), (uint32_t)x.d[i], m, t.mu[i]) : (uint32_t)x.d[i];
+        uint32_t v = theta ? mulmod((uint32_t)__ldg(pt + i), (uint32_t)y.d[i], m, t.mu[i]) : (uint32_t)y.d[i];
+        uint32_t a = fx > 0 ? u : (fx < 0 ? (u ? m - u : 0u) : 0u);
+        uint32_t b = fy > 0 ? v : (fy < 0 ? (v ? m - v : 0u) : 0u);
+        uint32_t s = reduce2(a + b, m);
+        if (sign) s = s ? m - s : 0u;
+        r.d[i] = (int)s;
+    }
+    if (sign) {
+        er_t lo = ev[0];
+        ev[0].frac = -ev[1].frac;
+        ev[0].exp = ev[1].exp;
+        ev[1].frac = -lo.frac;
+        ev[1].exp = lo.exp;
+    }
+    r.ev[0] = ev[0];
+    r.ev[1] = ev[1];
+    round_if_needed<N>(r);
+}
+
+/* cuda::mp_mul: mp_mul_common + rounding (src/arith/mul.cuh:53-113); also the
+ * split kernels mp_*_mul_esi/digits + round of src/mpvector.cuh, src/mpmatrix.cuh */
+template <int N> __device__ __forceinline__ void mp_mul(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y) {
+    const Tables<N> &t = T<N>();
+    r.exp = x.exp + y.exp;
+    r.sign = x.sign ^ y.sign;
+    r.ev[0] = er_md<false>(x.ev[0], y.ev[0], t.unit_upp);
+    r.ev[1] = er_md<true>(x.ev[1], y.ev[1], t.unit_low);
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = mulmod_i<N>(x.d[i], y.d[i], i);
+    round_if_needed<N>(r);
+}
+
+/* cuda::mp_mul_d, src/arith/muld.cuh:59-74 */
+template <int N> __device__ __forceinline__ void mp_mul_d(mp_t<N> &r, const mp_t<N> &x, double y) {
+    const Tables<N> &t = T<N>();
+    const uint64_t u = dbits(y);
+    const bool ynz = y != 0;
+    const uint64_t significand = ynz ? ((u & ((1ull << 52) - 1)) | (1ull << 52)) : 0ull;
+    const int yexp = (int)(((u >> 52) & 2047) - (ynz ? (uint64_t)(1023 + 52) : 0ull));
+    r.exp = x.exp + yexp;
+    r.sign = x.sign ^ (int)(u >> 63);
+    r.ev[0].exp = x.ev[0].exp;
+    r.ev[1].exp = x.ev[1].exp;
+    const double sd = (double)significand;
+    r.ev[0].frac = __dmul_rd(x.ev[0].frac, sd);
+    r.ev[1].frac = __dmul_ru(x.ev[1].frac, sd);
+    er_adjust(r.ev[0]);
+    er_adjust(r.ev[1]);
+    /* significand < 2^53: reduce it once per modulus, then multiply */
+    const uint32_t hi = (uint32_t)(significand >> 30), lo = (uint32_t)(significand & ((1u << 30) - 1));
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i];
+        /* significand mod m = (hi * 2^30 + lo) mod m, with hi < 2^23 */
+        uint32_t h = mulmod(hi, (uint32_t)(1u << 30), m, t.mu[i]);
+        uint32_t ym = reduce2(h + reduce2(lo, m), m);
+        r.d[i] = (int)mulmod((uint32_t)x.d[i], ym, m, t.mu[i]);
+    }
+    round_if_needed<N>(r);
+}
+
+/* ---------------------------- memory access ------------------------------ */
+
+/* element i of an SoA mp_array_t (src/types.cuh:85-92); len = *a.len */
+template <int N>
+__device__ __forceinline__ void load_soa(mp_t<N> &v, const int *digits, const int *sign, const int *exp,
+                                         const er_t *eval, int len, long long i) {
+    static_assert(N % 4 == 0, "vector loads of digits");
+    const int4 *dp = reinterpret_cast<const int4 *>(digits + (size_t)i * N);
+#pragma unroll
+    for (int q = 0; q < N / 4; q++) {
+        int4 w = __ldg(dp + q);
+        v.d[4 * q] = w.x; v.d[4 * q + 1] = w.y; v.d[4 * q + 2] = w.z; v.d[4 * q + 3] = w.w;
+    }
+    v.sign = __ldg(sign + i);
+    v.exp = __ldg(exp + i);
+    const longlong2 *ep = reinterpret_cast<const longlong2 *>(eval);
+    longlong2 lo = __ldg(ep + i), up = __ldg(ep + len + i);
+    v.ev[0].frac = __longlong_as_double(lo.x); v.ev[0].exp = lo.y;
+    v.ev[1].frac = __longlong_as_double(up.x); v.ev[1].exp = up.y;
+}
+template <int N>
+__device__ __forceinline__ void store_soa(const mp_t<N> &v, int *digits, int *sign, int *exp, er_t *eval, int len,
+                                          long long i) {
+    int4 *dp = reinterpret_cast<int4 *>(digits + (size_t)i * N);
+#pragma unroll
+    for (int q = 0; q < N / 4; q++) dp[q] = make_int4(v.d[4 * q], v.d[4 * q + 1], v.d[4 * q + 2], v.d[4 * q + 3]);
+    sign[i] = v.sign;
+    exp[i] = v.exp;
+    longlong2 *ep = reinterpret_cast<longlong2 *>(eval);
+    ep[i] = make_longlong2(__double_as_longlong(v.ev[0].frac), v.ev[0].exp);
+    ep[len + i] = make_longlong2(__double_as_longlong(v.ev[1].frac), v.ev[1].exp);
+}
+
+/* AoS mp_float_t (src/types.cuh:69-74): digits[N], sign, exp, eval[2]; 4N+40 bytes,
+ * 8-byte aligned.  Loaded as 8-byte words. */
+template <int N> __device__ __forceinline__ void load_aos(mp_t<N> &v, const void *base, long long i) {
+    const long long *p = reinterpret_cast<const long long *>((const char *)base + (size_t)i * (4 * N + 40));
+#pragma unroll
+    for (int q = 0; q < N / 2; q++) {
+        long long w = __ldg(p + q);
+        v.d[2 * q] = (int)(w & 0xffffffff);
+        v.d[2 * q + 1] = (int)(w >> 32);
+    }
+    long long se = __ldg(p + N / 2);
+    v.sign = (int)(se & 0xffffffff);
+    v.exp = (int)(se >> 32);
+    v.ev[0].frac = __longlong_as_double(__ldg(p + N / 2 + 1));
+    v.ev[0].exp = __ldg(p + N / 2 + 2);
+    v.ev[1].frac = __longlong_as_double(__ldg(p + N / 2 + 3));
+    v.ev[1].exp = __ldg(p + N / 2 + 4);
+}
+template <int N> __device__ __forceinline__ void store_aos(const mp_t<N> &v, void *base, long long i) {
+    long long *p = reinterpret_cast<long long *>((char *)base + (size_t)i * (4 * N + 40));
+#pragma unroll
+    for (int q = 0; q < N / 2; q++)
+        p[q] = (long long)(uint32_t)v.d[2 * q] | ((long long)(uint32_t)v.d[2 * q + 1] << 32);
+    p[N / 2] = (long long)(uint32_t)v.sign | ((long long)(uint32_t)v.exp << 32);
+    p[N / 2 + 1] = __double_as_longlong(v.ev[0].frac);
+    p[N / 2 + 2] = v.ev[0].exp;
+    p[N / 2 + 3] = __double_as_longlong(v.ev[1].frac);
+    p[N / 2 + 4] = v.ev[1].exp;
+}
+
+/* BLAS element index for a stride (negative strides start from the far end) */
+__device__ __forceinline__ long long blas_index(long long i, int n, int inc) {
+    return inc > 0 ? i * inc : ((long long)-n + i + 1) * inc;
+}
+
+} // namespace dev
+} // namespace mpres
+
+/* Per-translation-unit constant tables and their upload hook. */
+#define MPRES_DEFINE_TABLES(TU)                                                                        \
+    namespace mpres {                                                                                  \
+    namespace {                                                                                        \
+    __constant__ Tables<8> g_tab8;                                                                     \
+    __constant__ Tables<16> g_tab16;                                                                   \
+    __constant__ Tables<32> g_tab32;                                                                   \
+    }                                                                                                  \
+    namespace dev {                                                                                    \
+    template <> __device__ __forceinline__ const Tables<8> &T<8>() { return g_tab8; }                  \
+    template <> __device__ __forceinline__ const Tables<16> &T<16>() { return g_tab16; }               \
+    template <> __device__ __forceinline__ const Tables<32> &T<32>() { return g_tab32; }               \
+    }                                                                                                  \
+    cudaError_t upload_tables_##TU(int n, const void *tab) {                                           \
+        if (n == 8) return cudaMemcpyToSymbol(g_tab8, tab, sizeof(Tables<8>));                         \
+        if (n == 16) return cudaMemcpyToSymbol(g_tab16, tab, sizeof(Tables<16>));                      \
+        if (n == 32) return cudaMemcpyToSymbol(g_tab32, tab, sizeof(Tables<32>));                      \
+        return cudaErrorInvalidValue;                                                                  \
+    }                                                                                                  \
+    }
+
+#endif

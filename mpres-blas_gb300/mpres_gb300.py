@@ -1,0 +1,312 @@
+"""Python access to libmpres_gb300.so through its C ABI (include/mpres_gb300.h).
+
+This is plumbing for tests and benchmarks: it loads the in-tree CUDA library,
+raises on any error status, and moves numpy arrays in the reference's
+mp_float_t layout to and from device memory.  There is no CPU fallback: if the
+library or a GPU is missing, the calls fail loudly.
+"""
+import ctypes
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libmpres_gb300.so"
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+SZ = ctypes.c_size_t
+
+NO_TRANS, TRANS = 111, 112
+ER = np.dtype([("frac", "<f8"), ("exp", "<i8")])
+
+
+def mp_dtype(n):
+    """mp_float_t for n moduli (src/types.cuh:69-74), 4n + 40 bytes."""
+    return np.dtype([("digits", "<i4", (n,)), ("sign", "<i4"), ("exp", "<i4"), ("eval", ER, (2,))])
+
+
+class MpArrayT(ctypes.Structure):
+    _fields_ = [("digits", P), ("sign", P), ("exp", P), ("eval", P), ("buf", P), ("len", P)]
+
+
+class CsrT(ctypes.Structure):
+    _fields_ = [("as_", P), ("ja", P), ("irp", P)]
+
+
+class EllT(ctypes.Structure):
+    _fields_ = [("as_", P), ("ja", P)]
+
+
+class MpresError(RuntimeError):
+    pass
+
+
+_SIGS = {
+    "mpres_last_error": (ctypes.c_char_p, []),
+    "mpres_mp_float_size": (SZ, [I]),
+    "mpres_init": (I, [I]),
+    "mpres_get_int_constants": (I, [I, P]),
+    "mpres_array_init": (I, [I, P, SZ]),
+    "mpres_array_clear": (I, [P]),
+    "mpres_array_host2device": (I, [I, P, P, SZ]),
+    "mpres_array_device2host": (I, [I, P, P, SZ]),
+    "mpres_csr_init": (I, [P, I, I]),
+    "mpres_csr_host2device": (I, [P, P, I, I]),
+    "mpres_csr_clear": (I, [P]),
+    "mpres_ell_init": (I, [P, I, I]),
+    "mpres_ell_host2device": (I, [P, P, I, I]),
+    "mpres_ell_clear": (I, [P]),
+    "mpres_set_d": (I, [I, P, SZ, P]),
+    "mpres_dot": (I, [I, I, P, I, P, I, P, P, I, I, I, I, I, P]),
+    "mpres_gemv": (I, [I, I, I, I, P, P, I, P, I, P, P, I, P, P, I, I, I, I, P]),
+    "mpres_gemm": (I, [I, I, I, I, I, I, P, P, I, P, I, P, P, I, P, I, I, I, I, I, P]),
+    "mpres_spmv_csr": (I, [I, I, P, P, P, I, P]),
+    "mpres_spmv_csrv": (I, [I, I, P, P, P, I, I, P]),
+    "mpres_spmv_ell": (I, [I, I, I, P, P, P, I, P]),
+    "mpres_probe_mulmod": (I, [I, I, ctypes.c_longlong, P, P]),
+    "mpres_probe_dadd": (I, [I, I, ctypes.c_longlong, P, P]),
+    "mpres_elementwise": (I, [I, I, P, P, P, SZ, P]),
+    "mpres_probe_ceil_log2": (I, [P, P, SZ, P]),
+    "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
+    "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise MpresError("libmpres_gb300.so not built: run __graft_entry__.build() or mpres-blas_gb300/build.py")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc, what=""):
+    if rc != 0:
+        msg = lib().mpres_last_error().decode()
+        raise MpresError("%s failed (status %d): %s" % (what, rc, msg))
+
+
+def init(nmod):
+    check(lib().mpres_init(nmod), "mpres_init")
+
+
+def int_constants(nmod):
+    out = (ctypes.c_int * 5)()
+    check(lib().mpres_get_int_constants(nmod, out), "mpres_get_int_constants")
+    return dict(mp_precision=out[0], mp_h=out[1], mp_j=out[2], ref_factor=out[3], log2m=out[4])
+
+
+def set_d(nmod, x):
+    """Host conversion of doubles (the reference's mp_set_d)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros(x.size, mp_dtype(nmod))
+    check(lib().mpres_set_d(nmod, x.ctypes.data, x.size, out.ctypes.data), "mpres_set_d")
+    return out
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+class DeviceArray:
+    """An mp_array_t (SoA) in device memory, allocated by mpres_array_init."""
+
+    def __init__(self, nmod, size):
+        self.nmod, self.size = nmod, size
+        self.a = MpArrayT()
+        check(lib().mpres_array_init(nmod, ctypes.byref(self.a), size), "mpres_array_init")
+        self._live = True
+
+    @classmethod
+    def from_host(cls, nmod, host):
+        d = cls(nmod, len(host))
+        d.upload(host)
+        return d
+
+    def upload(self, host):
+        host = np.ascontiguousarray(host)
+        assert host.dtype.itemsize == 4 * self.nmod + 40 and len(host) == self.size
+        check(lib().mpres_array_host2device(self.nmod, ctypes.byref(self.a), host.ctypes.data, self.size),
+              "mpres_array_host2device")
+
+    def download(self):
+        out = np.zeros(self.size, mp_dtype(self.nmod))
+        check(lib().mpres_array_device2host(self.nmod, out.ctypes.data, ctypes.byref(self.a), self.size),
+              "mpres_array_device2host")
+        return out
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.a)
+
+    def free(self):
+        if self._live:
+            check(lib().mpres_array_clear(ctypes.byref(self.a)), "mpres_array_clear")
+            self._live = False
+
+    def __del__(self):
+        try:
+            if self._live and _lib is not None:
+                _lib.mpres_array_clear(ctypes.byref(self.a))
+                self._live = False
+        except Exception:
+            pass
+
+
+class DeviceBytes:
+    """Raw device memory for AoS mp_float_t vectors (the SpMV operands), held as a
+    torch uint8 tensor so that torch's allocator owns it."""
+
+    def __init__(self, nbytes, device="cuda"):
+        import torch
+        self.t = torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+        self.nbytes = int(nbytes)
+
+    @property
+    def ptr(self):
+        return self.t.data_ptr()
+
+    @classmethod
+    def from_numpy(cls, arr):
+        import torch
+        arr = np.ascontiguousarray(arr)
+        d = cls(arr.nbytes)
+        if arr.nbytes:
+            d.t[: arr.nbytes].copy_(torch.from_numpy(arr.view(np.uint8).reshape(-1)))
+        return d
+
+    def to_numpy(self, dtype, count):
+        raw = self.t[: np.dtype(dtype).itemsize * count].cpu().numpy()
+        return raw.view(dtype).copy()
+
+
+class DeviceCsr:
+    def __init__(self, m, irp, ja, vals):
+        irp = np.ascontiguousarray(irp, dtype=np.int32)
+        ja = np.ascontiguousarray(ja, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.m, self.nnz = m, len(ja)
+        self.c = CsrT()
+        check(lib().mpres_csr_init(ctypes.byref(self.c), m, self.nnz), "mpres_csr_init")
+        host = CsrT(vals.ctypes.data, ja.ctypes.data, irp.ctypes.data)
+        check(lib().mpres_csr_host2device(ctypes.byref(self.c), ctypes.byref(host), m, self.nnz),
+              "mpres_csr_host2device")
+        self._live = True
+
+    def free(self):
+        if self._live:
+            check(lib().mpres_csr_clear(ctypes.byref(self.c)), "mpres_csr_clear")
+            self._live = False
+
+
+class DeviceEll:
+    def __init__(self, m, maxnzr, ja, vals):
+        ja = np.ascontiguousarray(ja, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        self.m, self.maxnzr = m, maxnzr
+        self.e = EllT()
+        check(lib().mpres_ell_init(ctypes.byref(self.e), m, maxnzr), "mpres_ell_init")
+        host = EllT(vals.ctypes.data, ja.ctypes.data)
+        check(lib().mpres_ell_host2device(ctypes.byref(self.e), ctypes.byref(host), m, maxnzr),
+              "mpres_ell_host2device")
+        self._live = True
+
+    def free(self):
+        if self._live:
+            check(lib().mpres_ell_clear(ctypes.byref(self.e)), "mpres_ell_clear")
+            self._live = False
+
+
+def dot(nmod, n, x, y, r, incx=1, incy=1, order=(512, 128, 8192, 256, 64), buffer=None, stream=None):
+    """cuda::mp_dot<g1,b1,g2,g3,b3>(n, x, incx, y, incy, r, buffer); order = the template arguments."""
+    g1, b1, g2, g3, b3 = order
+    check(lib().mpres_dot(nmod, n, x.ref, incx, y.ref, incy, r.ref, buffer.ref if buffer else None,
+                          g1, b1, g2, g3, b3, _stream_handle(stream)), "mpres_dot")
+
+
+def gemv(nmod, trans, m, n, alpha, A, lda, x, beta, y, incx=1, incy=1, order=(256, 128, 256, 32), stream=None):
+    """cuda::mp_gemv<g1,b1,g2,b3>(trans, m, n, alpha, A, lda, x, incx, beta, y, incy, buf1, buf2)."""
+    g1, b1, g2, b3 = order
+    check(lib().mpres_gemv(nmod, trans, m, n, alpha.ref, A.ref, lda, x.ref, incx, beta.ref, y.ref, incy, None, None,
+                           g1, b1, g2, b3, _stream_handle(stream)), "mpres_gemv")
+
+
+def gemm(nmod, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, transa=NO_TRANS, transb=NO_TRANS,
+         order=(32, 1, 128, 64, 16), stream=None):
+    """cuda::mp_gemm<b1x,b1y,g2x,g2y,b3>(transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, buffer)."""
+    b1x, b1y, g2x, g2y, b3 = order
+    check(lib().mpres_gemm(nmod, transa, transb, m, n, k, alpha.ref, A.ref, lda, B.ref, ldb, beta.ref, C.ref, ldc,
+                           None, b1x, b1y, g2x, g2y, b3, _stream_handle(stream)), "mpres_gemm")
+
+
+def spmv_csr(nmod, m, csr, x, y, threads=32, stream=None):
+    check(lib().mpres_spmv_csr(nmod, m, ctypes.byref(csr.c), x.ptr, y.ptr, threads, _stream_handle(stream)),
+          "mpres_spmv_csr")
+
+
+def spmv_csrv(nmod, m, csr, x, y, tpr, threads=32, stream=None):
+    check(lib().mpres_spmv_csrv(nmod, m, ctypes.byref(csr.c), x.ptr, y.ptr, threads, tpr, _stream_handle(stream)),
+          "mpres_spmv_csrv")
+
+
+def spmv_ell(nmod, m, ell, x, y, threads=32, stream=None):
+    check(lib().mpres_spmv_ell(nmod, m, ell.maxnzr, ctypes.byref(ell.e), x.ptr, y.ptr, threads,
+                               _stream_handle(stream)), "mpres_spmv_ell")
+
+
+OP_ADD, OP_MUL, OP_MUL_D = 0, 1, 2
+
+
+def elementwise(nmod, op, x, y):
+    """Element-wise device arithmetic on host numpy records (copies in and out)."""
+    import torch
+    dx = DeviceBytes.from_numpy(x)
+    dy = DeviceBytes.from_numpy(y)
+    dr = DeviceBytes(x.nbytes)
+    check(lib().mpres_elementwise(nmod, op, dx.ptr, dy.ptr, dr.ptr, len(x), None), "mpres_elementwise")
+    torch.cuda.synchronize()
+    return dr.to_numpy(x.dtype, len(x))
+
+
+def rns_scale2pow(nmod, digits, D):
+    import torch
+    digits = np.ascontiguousarray(digits, dtype=np.int32)
+    D = np.ascontiguousarray(D, dtype=np.uint32)
+    dd, dD, do = DeviceBytes.from_numpy(digits), DeviceBytes.from_numpy(D), DeviceBytes(digits.nbytes)
+    check(lib().mpres_rns_scale2pow(nmod, dd.ptr, dD.ptr, do.ptr, D.size, None), "mpres_rns_scale2pow")
+    torch.cuda.synchronize()
+    return do.to_numpy(np.int32, digits.size).reshape(digits.shape)
+
+
+def rns_eval(nmod, digits, fast):
+    import torch
+    digits = np.ascontiguousarray(digits, dtype=np.int32)
+    cnt = digits.size // nmod
+    dd, lo, up = DeviceBytes.from_numpy(digits), DeviceBytes(16 * cnt), DeviceBytes(16 * cnt)
+    check(lib().mpres_rns_eval(nmod, int(fast), dd.ptr, lo.ptr, up.ptr, cnt, None), "mpres_rns_eval")
+    torch.cuda.synchronize()
+    return lo.to_numpy(ER, cnt), up.to_numpy(ER, cnt)
+
+
+def probe_ceil_log2(x):
+    """ceil(log2(x)) evaluated on the GPU with the CUDA math library."""
+    import torch
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    dx, do = DeviceBytes.from_numpy(x), DeviceBytes(x.nbytes)
+    check(lib().mpres_probe_ceil_log2(dx.ptr, do.ptr, x.size, None), "mpres_probe_ceil_log2")
+    torch.cuda.synchronize()
+    return do.to_numpy(np.float64, x.size)

@@ -1,0 +1,253 @@
+"""Parity of the CUDA library with the reference: every result bit-identical (digits,
+sign, exponent and interval evaluation) to the golden vectors made by the
+reference itself and to the oracle, from small edge cases up to the benchmark
+sizes.  All calls go through the C ABI."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import helpers
+from oracle import ffi
+
+pytestmark = pytest.mark.gpu
+GOLD = helpers.ROOT / "tests" / "golden"
+
+
+def sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+def eq(a, b):
+    mm = ffi.mismatches(a, b)
+    assert len(mm) == 0, "%d of %d records differ, first at %d" % (len(mm), len(a), mm[0])
+
+
+def run_dot(lib, n, mx, my, count, order, incx=1, incy=1, r0=None):
+    x, y = lib.DeviceArray.from_host(n, mx), lib.DeviceArray.from_host(n, my)
+    r = lib.DeviceArray(n, 1)
+    if r0 is not None:
+        r.upload(r0)
+    lib.dot(n, count, x, y, r, incx=incx, incy=incy, order=order)
+    sync()
+    return r.download()
+
+
+# ------------------------------------------------------------------ DOT ----
+
+@pytest.mark.parametrize("name,n", [("dot_8.npz", 8), ("dot_16.npz", 16), ("dot_32.npz", 32)])
+def test_dot_golden(gpu, name, n):
+    g = np.load(GOLD / name)
+    for tag in sorted({k.rsplit("_", 1)[0] for k in g.files}):
+        count, incx, incy, g1, b1, g2, g3, b3 = [int(v) for v in g[tag + "_meta"]]
+        r = run_dot(gpu, n, g[tag + "_mx"], g[tag + "_my"], count, (g1, b1, g2, g3, b3), incx, incy)
+        eq(r, g[tag + "_r"])
+
+
+@pytest.mark.parametrize("n,count,order", [
+    (8, 1 << 16, (512, 128, 8192, 256, 64)),
+    (8, 100003, (1, 1, 1, 64, 64)),
+    (8, 50000, (1, 1, 1, 37, 200)),
+    (8, 4000, (1, 1, 1, 2, 1024)),
+    (16, 30000, (512, 128, 8192, 256, 64)),
+    (32, 20000, (512, 128, 8192, 96, 32)),
+])
+def test_dot_random_vs_oracle(gpu, oracle, n, count, order):
+    rng = np.random.default_rng(helpers.SEED + count + n)
+    mx = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    my = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    r = run_dot(gpu, n, mx, my, count, order)
+    eq(r, oracle.dot(n, mx, my, g3=order[3], b3=order[4]))
+
+
+def test_dot_strides_and_reuse(gpu, oracle):
+    rng = np.random.default_rng(helpers.SEED + 11)
+    count = 3000
+    mx = gpu.set_d(8, helpers.doubles(rng, 1 + (count - 1) * 3, -16, 16))
+    my = gpu.set_d(8, helpers.doubles(rng, 1 + (count - 1) * 2, -16, 16))
+    for incx, incy in [(3, 2), (-3, 2), (3, -2), (-3, -2)]:
+        r = run_dot(gpu, 8, mx, my, count, (1, 1, 1, 48, 64), incx, incy)
+        eq(r, oracle.dot(8, mx, my, g3=48, b3=64, incx=incx, incy=incy, length=count))
+
+
+def test_dot_zero_length_leaves_result(gpu):
+    rec = gpu.set_d(8, np.array([1.5]))
+    r = run_dot(gpu, 8, rec, rec, 0, (512, 128, 8192, 256, 64), r0=rec)
+    eq(r, rec)
+
+
+def test_dot_full_size(gpu, oracle):
+    """n = 2^20, x and y = u*2^e with e in -16..16: the size and distribution of the
+    DOT benchmark, bit-identical to the oracle at the reference's launch parameters."""
+    rng = np.random.default_rng(helpers.SEED + 0)
+    count = 1 << 20
+    mx = gpu.set_d(8, helpers.doubles(rng, count, -16, 16))
+    my = gpu.set_d(8, helpers.doubles(rng, count, -16, 16))
+    r = run_dot(gpu, 8, mx, my, count, (512, 128, 8192, 256, 64))
+    eq(r, oracle.dot(8, mx, my, g3=256, b3=64))
+
+
+# ----------------------------------------------------------------- GEMV ----
+
+def run_gemv(lib, n, trans, m, cols, alpha, A, lda, x, beta, y, incx, incy, b3):
+    dA, dx, dy = (lib.DeviceArray.from_host(n, v) for v in (A, x, y))
+    da, db = lib.DeviceArray.from_host(n, alpha), lib.DeviceArray.from_host(n, beta)
+    lib.gemv(n, trans, m, cols, da, dA, lda, dx, db, dy, incx=incx, incy=incy, order=(256, 128, 256, b3))
+    sync()
+    return dy.download()
+
+
+@pytest.mark.parametrize("name,n", [("gemv_16.npz", 16), ("gemv_8.npz", 8)])
+def test_gemv_golden(gpu, name, n):
+    g = np.load(GOLD / name)
+    for tag in sorted({k.rsplit("_", 1)[0] for k in g.files}):
+        trans, m, cols, lda, incx, incy, b3 = [int(v) for v in g[tag + "_meta"]]
+        r = run_gemv(gpu, n, trans, m, cols, g[tag + "_alpha"], g[tag + "_A"], lda, g[tag + "_x"],
+                     g[tag + "_beta"], g[tag + "_y"], incx, incy, b3)
+        eq(r, g[tag + "_r"])
+
+
+@pytest.mark.parametrize("n,trans,m,cols,b3", [
+    (16, 111, 300, 200, 32), (16, 112, 260, 190, 32), (16, 111, 33, 1000, 256), (8, 112, 500, 45, 7),
+    (32, 111, 64, 130, 32), (16, 111, 1, 1, 32), (16, 112, 100, 3, 600),
+])
+def test_gemv_random_vs_oracle(gpu, oracle, n, trans, m, cols, b3):
+    rng = np.random.default_rng(helpers.SEED + 3 + m + cols)
+    lda = m + 2
+    lx, ly = (cols, m) if trans == 111 else (m, cols)
+    A = gpu.set_d(n, helpers.doubles(rng, lda * cols, -32, 32))
+    x = gpu.set_d(n, helpers.doubles(rng, lx, -32, 32))
+    y = gpu.set_d(n, helpers.doubles(rng, ly, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    r = run_gemv(gpu, n, trans, m, cols, al, A, lda, x, be, y, 1, 1, b3)
+    eq(r, oracle.gemv(n, trans, m, cols, al, A, lda, x, be, y, b3=b3))
+
+
+# ----------------------------------------------------------------- GEMM ----
+
+def run_gemm(lib, n, m, cols, k, alpha, A, lda, B, ldb, beta, C, ldc):
+    dA, dB, dC = (lib.DeviceArray.from_host(n, v) for v in (A, B, C))
+    da, db = lib.DeviceArray.from_host(n, alpha), lib.DeviceArray.from_host(n, beta)
+    lib.gemm(n, m, cols, k, da, dA, lda, dB, ldb, db, dC, ldc)
+    sync()
+    return dC.download()
+
+
+@pytest.mark.parametrize("name,n", [("gemm_32.npz", 32), ("gemm_8.npz", 8)])
+def test_gemm_golden(gpu, name, n):
+    g = np.load(GOLD / name)
+    for tag in sorted({k.rsplit("_", 1)[0] for k in g.files}):
+        m, cols, k, lda, ldb, ldc = [int(v) for v in g[tag + "_meta"]]
+        r = run_gemm(gpu, n, m, cols, k, g[tag + "_alpha"], g[tag + "_A"], lda, g[tag + "_B"], ldb,
+                     g[tag + "_beta"], g[tag + "_C"], ldc)
+        eq(r, g[tag + "_r"])
+
+
+@pytest.mark.parametrize("n,m,cols,k", [(32, 40, 30, 60), (8, 70, 33, 129), (16, 37, 41, 17)])
+def test_gemm_random_vs_oracle(gpu, oracle, n, m, cols, k):
+    rng = np.random.default_rng(helpers.SEED + 1 + m * cols)
+    lda, ldb, ldc = m, k, m
+    A = gpu.set_d(n, helpers.doubles(rng, lda * k, -32, 32))
+    B = gpu.set_d(n, helpers.doubles(rng, ldb * cols, -32, 32))
+    C = gpu.set_d(n, helpers.doubles(rng, ldc * cols, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    r = run_gemm(gpu, n, m, cols, k, al, A, lda, B, ldb, be, C, ldc)
+    eq(r, oracle.gemm(n, m, cols, k, al, A, lda, B, ldb, be, C, ldc))
+
+
+def test_gemm_transposed_is_not_supported(gpu):
+    rec = gpu.set_d(8, np.ones(4))
+    d = gpu.DeviceArray.from_host(8, rec)
+    a = gpu.DeviceArray.from_host(8, rec[:1])
+    with pytest.raises(gpu.MpresError):
+        gpu.gemm(8, 2, 2, 2, a, d, 2, d, 2, a, d, 2, transa=gpu.TRANS)
+
+
+def test_gemm_full_size_sampled(gpu, oracle):
+    """m = n = k = 1024 with 32 moduli (the GEMM benchmark): entries checked
+    bit-for-bit against the oracle on a sample of 24 outputs (each one is a
+    1024-long chain, computed by the oracle on the row/column it depends on)."""
+    n, m = 32, 1024
+    rng = np.random.default_rng(helpers.SEED + 1)
+    A = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    B = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    C = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    r = run_gemm(gpu, n, m, m, m, al, A, m, B, m, be, C, m)
+    for _ in range(24):
+        row, col = (int(v) for v in rng.integers(0, m, 2))
+        arow = np.ascontiguousarray(A[row::m])  # A(row, :) with stride lda = m
+        bcol = np.ascontiguousarray(B[col * m:(col + 1) * m])
+        c = C[row + col * m:row + col * m + 1].copy()
+        want = oracle.gemm(n, 1, 1, m, al, arow, 1, bcol, m, be, c, 1)
+        eq(r[row + col * m:row + col * m + 1], want)
+
+
+# ----------------------------------------------------------------- SpMV ----
+
+def run_spmv(lib, n, kind, m, mx, irp=None, ja=None, vals=None, tpr=None, maxnzr=None, ell_ja=None, ell_as=None):
+    x = lib.DeviceBytes.from_numpy(mx)
+    y = lib.DeviceBytes(m * mx.dtype.itemsize)
+    if kind == "ell":
+        e = lib.DeviceEll(m, maxnzr, ell_ja, ell_as)
+        lib.spmv_ell(n, m, e, x, y)
+    else:
+        c = lib.DeviceCsr(m, irp, ja, vals)
+        if kind == "csr":
+            lib.spmv_csr(n, m, c, x, y)
+        else:
+            lib.spmv_csrv(n, m, c, x, y, tpr)
+    sync()
+    return y.to_numpy(mx.dtype, m)
+
+
+def test_spmv_golden(gpu):
+    g = np.load(GOLD / "spmv_8.npz")
+    m = len(g["irp"]) - 1
+    eq(run_spmv(gpu, 8, "csr", m, g["mx"], g["irp"], g["ja"], g["vals"]), g["csr"])
+    for tpr in (1, 2, 4, 8, 16, 32):
+        eq(run_spmv(gpu, 8, "csrv", m, g["mx"], g["irp"], g["ja"], g["vals"], tpr=tpr), g["csrv%d" % tpr])
+    eq(run_spmv(gpu, 8, "ell", m, g["mx"], maxnzr=int(g["maxnzr"][0]), ell_ja=g["ell_ja"], ell_as=g["ell_as"]),
+       g["ell"])
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_spmv_random_vs_oracle(gpu, oracle, n):
+    rng = np.random.default_rng(helpers.SEED + 2 + n)
+    m = 20000
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
+    mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
+    eq(run_spmv(gpu, n, "csr", m, mx, irp, ja, vals), oracle.spmv_csr(n, m, irp, ja, vals, mx))
+    for tpr in (4, 16, 32):
+        eq(run_spmv(gpu, n, "csrv", m, mx, irp, ja, vals, tpr=tpr), oracle.spmv_csrv(n, m, tpr, irp, ja, vals, mx))
+    small = 3000
+    sirp, sja, svals = helpers.random_csr(rng, small, m, helpers.power_law_rows(rng, small, kmax=200))
+    maxnzr, eja, eas = helpers.csr_to_ell(small, sirp, sja, svals)
+    eq(run_spmv(gpu, n, "ell", small, mx, maxnzr=maxnzr, ell_ja=eja, ell_as=eas),
+       oracle.spmv_ell(n, small, maxnzr, eja, eas, mx))
+
+
+def test_spmv_full_size(gpu, oracle):
+    """2^20 rows, power-law row lengths 1..1024 (mean 16): the SpMV benchmark, all
+    outputs bit-identical to the oracle for CSR and CSR-vector with 32 lanes."""
+    rng = np.random.default_rng(helpers.SEED + 2)
+    m = 1 << 20
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
+    mx = gpu.set_d(8, helpers.doubles(rng, m, -16, 16))
+    eq(run_spmv(gpu, 8, "csr", m, mx, irp, ja, vals), oracle.spmv_csr(8, m, irp, ja, vals, mx))
+    eq(run_spmv(gpu, 8, "csrv", m, mx, irp, ja, vals, tpr=32), oracle.spmv_csrv(8, m, 32, irp, ja, vals, mx))
+
+
+# ---------------------------------------------------------------- errors ----
+
+def test_bad_arguments_are_reported(gpu):
+    rec = gpu.set_d(8, np.ones(4))
+    d = gpu.DeviceArray.from_host(8, rec)
+    with pytest.raises(gpu.MpresError):
+        gpu.dot(8, 4, d, d, d, order=(1, 1, 1, 0, 64))
+    c = gpu.DeviceCsr(2, np.array([0, 1, 2]), np.array([0, 1]), np.array([1.0, 2.0]))
+    x = gpu.DeviceBytes.from_numpy(rec)
+    with pytest.raises(gpu.MpresError):
+        gpu.spmv_csrv(8, 2, c, x, x, tpr=3)
+    assert gpu.lib().mpres_dot(12, 4, d.ref, 1, d.ref, 1, d.ref, None, 1, 1, 1, 1, 1, None) != 0
