@@ -30,6 +30,7 @@
 #endif
 
 #include "../mpres-blas_gb300/csrc/moduli_sets.h"
+#include "cuda_log2_table.h"
 
 typedef ora_er_t er_t;
 
@@ -485,13 +486,56 @@ static void rns_mul(const ora_ctx_t *c, int *r, const int *x, const int *y) {
     for (int i = 0; i < c->n; i++) r[i] = mod_mul(x[i], y[i], c->moduli[i]);
 }
 
+/* ceil(log2(x)) as the reference's DEVICE code obtains it (CUDA's log2,
+ * src/rns.cuh:848, :913): the exact ceiling, corrected within a few ulps of a
+ * power of two by the deviations of CUDA's log2 measured on the GPU
+ * (cuda_log2_table.h, made by gen_cuda_log2_table.py). */
+static double exact_ceil_log2(double x) {
+    int e;
+    double m = frexp(x, &e); /* x = m * 2^e, m in [0.5, 1) */
+    return (m == 0.5) ? e - 1 : e;
+}
+static int log2_row_lo[2100], log2_row_hi[2100]; /* rows of each binade in the table */
+static int log2_index_ready;
+static void log2_index(void) {
+    for (int i = 0; i < 2100; i++) log2_row_lo[i] = log2_row_hi[i] = 0;
+    for (int r = 0; r < ORA_CUDA_LOG2_RUNS; r++) {
+        int b = ORA_CUDA_LOG2_TABLE[r][0] + 1074;
+        if (log2_row_hi[b] == 0) log2_row_lo[b] = r;
+        log2_row_hi[b] = r + 1;
+    }
+    log2_index_ready = 1;
+}
+static int log2_delta(int e, int64_t steps) {
+    if (e < -1074 || e > 1023) return 0;
+    int b = e + 1074;
+    for (int r = log2_row_lo[b]; r < log2_row_hi[b]; r++)
+        if (steps >= ORA_CUDA_LOG2_TABLE[r][1] && steps <= ORA_CUDA_LOG2_TABLE[r][2]) return ORA_CUDA_LOG2_TABLE[r][3];
+    return 0;
+}
+static double dev_ceil_log2(double x) {
+    if (!log2_index_ready) {
+#pragma omp critical(ora_log2)
+        if (!log2_index_ready) log2_index();
+    }
+    int e;
+    frexp(x, &e);
+    e -= 1; /* 2^e <= x < 2^(e+1) */
+    int64_t bx = (int64_t)bits_of(x);
+    int64_t below = bx - (int64_t)bits_of(ldexp(1.0, e));       /* steps above 2^e, >= 0 */
+    int64_t above = bx - (int64_t)bits_of(ldexp(1.0, e + 1));   /* steps below 2^(e+1), < 0 */
+    int d = log2_delta(e, below);
+    if (!d) d = log2_delta(e + 1, above);
+    return exact_ceil_log2(x) + d;
+}
+
 /* the refinement loop shared by rns_eval_compute[_fast] (src/rns.cuh:843-867, :908-932) */
 static void eval_refine(const ora_ctx_t *c, int *s, double sumu, er_t *low, er_t *upp) {
     const int n = c->n;
     double fracl[ORA_MAXN], fracu[ORA_MAXN];
     int K = 0;
     while (sumu < c->eval_acc) {
-        double a = -(ceil(log2(sumu)) + 1);
+        double a = -(dev_ceil_log2(sumu) + 1);
         int k = (int)(a > c->ref_factor ? a : c->ref_factor);
         rns_mul(c, s, s, &c->pow2[k * n]);
         for (int i = 0; i < n; i++) fracu[i] = mul_ru(s[i], c->recip_ru[i]);
@@ -655,7 +699,7 @@ static inline int pow2_row(const ora_ctx_t *c, int idx) {
 /* src/arith/arith_utils.cuh:197-206 (cuda::sign_estimate) */
 static int sign_estimate(const ora_ctx_t *c, const int *dx, const int *dy, int sx, int sy, int gamma, int theta,
                          int nzx, int nzy) {
-    int lx[ORA_MAXN], ly[ORA_MAXN];
+    int lx[ORA_MAXN] = {0}, ly[ORA_MAXN] = {0};
     const int *pg = &c->pow2[pow2_row(c, gamma) * c->n], *pt = &c->pow2[pow2_row(c, theta) * c->n];
     for (int i = 0; i < c->n; i++) {
         lx[i] = nzx * mod_mul(dx[i], pg[i], c->moduli[i]);

@@ -28,7 +28,7 @@ for N in ${REF_SETS:-8 16 32}; do
     PARAMS="$REF_SRC/params/32-bit-moduli/params.${N}_32bit.h"
     g++ -std=c++17 -O2 -fPIC -shared -w \
         -frounding-math -fno-fast-math -ffp-contract=off \
-        -I"$REF_SRC" -I"$HERE/shim" -I"$HERE" \
+        -I"$REF_SRC" -I"$HERE/shim" -I"$HERE" -I"$ORACLE" \
         -include "$PARAMS" \
         "$HERE/ref_harness.cpp" -o "$OUT/libmpres_ref_${N}.so" \
         "$MPFR" "$GMP" &

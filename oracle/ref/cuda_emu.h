@@ -90,6 +90,36 @@ ORACLE_DIRECTED(__ddiv_rd, /, FE_DOWNWARD)
 ORACLE_DIRECTED(__ddiv_ru, /, FE_UPWARD)
 #undef ORACLE_DIRECTED
 
+/* ---- CUDA's log2 as the device code sees it ----
+ * The reference's device code uses log2 only for ceil(log2(sumu)) in its
+ * interval-evaluation refinement loop (src/rns.cuh:848, :913).  CUDA's log2 can
+ * be one ulp off the exact value within a few ulps of a power of two, which
+ * changes that ceiling; cuda_log2_table.h lists those deviations as measured on
+ * the GPU.  Unqualified calls inside namespace cuda resolve to this function,
+ * which returns a value whose ceiling is CUDA's; host code keeps the C library's. */
+#include "cuda_log2_table.h"
+namespace emu_log2 {
+    inline int delta(int e, long long steps) {
+        for (int r = 0; r < ORA_CUDA_LOG2_RUNS; r++)
+            if (ORA_CUDA_LOG2_TABLE[r][0] == e && steps >= ORA_CUDA_LOG2_TABLE[r][1] &&
+                steps <= ORA_CUDA_LOG2_TABLE[r][2])
+                return ORA_CUDA_LOG2_TABLE[r][3];
+        return 0;
+    }
+    inline long long bits(double d) { long long u; memcpy(&u, &d, 8); return u; }
+}
+namespace cuda {
+    inline double log2(double x) {
+        int e;
+        double m = frexp(x, &e);
+        double exact = (m == 0.5) ? e - 1 : e;
+        e -= 1;
+        int d = emu_log2::delta(e, emu_log2::bits(x) - emu_log2::bits(ldexp(1.0, e)));
+        if (!d) d = emu_log2::delta(e + 1, emu_log2::bits(x) - emu_log2::bits(ldexp(1.0, e + 1)));
+        return exact + d - 0.5;
+    }
+}
+
 /* ---- block execution: one coroutine per thread, __syncthreads() yields ---- */
 namespace emu {
     struct Block {

@@ -69,3 +69,46 @@ def test_host_conversion_matches_oracle(library, oracle, n):
 def test_unsupported_set_is_an_error(library):
     with pytest.raises(library.MpresError):
         library.set_d(12, np.ones(3))
+
+
+DRIVER = r"""
+#define RNS_MODULI_SIZE 8
+#include "mpres_gb300.hpp"
+#include <vector>
+/* the calling sequence of the reference's benchmark drivers
+ * (tests/blas/performance/test_dot_performance.cu, tests/sparse/spmv/csr/test_mpres_spmv_csr.cuh) */
+int main() {
+    rns_const_init();
+    mp_const_init();
+    const int n = 1000;
+    std::vector<mp_float_t> hx(n), hy(n), hr(1);
+    mp_array_t x, y, r, buf;
+    cuda::mp_array_init(x, n); cuda::mp_array_init(y, n); cuda::mp_array_init(r, 1); cuda::mp_array_init(buf, n);
+    cuda::mp_array_host2device(x, hx.data(), n);
+    cuda::mp_array_host2device(y, hy.data(), n);
+    cuda::mp_dot<512, 128, 8192, 256, 64>(n, x, 1, y, 1, r, buf);
+    cuda::mp_gemv<256, 128, 256, 32>(mblas_no_trans, 10, 100, r, x, 10, y, 1, r, y, 1, buf, buf);
+    cuda::mp_gemm<32, 1, 128, 64, 16>(mblas_no_trans, mblas_no_trans, 10, 10, 10, r, x, 10, y, 10, r, x, 10, buf);
+    csr_t csr;
+    cuda::csr_init(csr, 10, 10);
+    cuda::mp_spmv_csr<32>(10, csr, hx.data(), hy.data());
+    cuda::mp_spmv_csrv<32, 4>(10, csr, hx.data(), hy.data());
+    cuda::csr_clear(csr);
+    cuda::mp_array_device2host(hr.data(), r, 1);
+    cuda::mp_array_clear(x);
+    return 0;
+}
+"""
+
+
+def test_cpp_dropin_header_compiles_and_links(library, tmp_path):
+    """A driver written like the reference's own, against include/mpres_gb300.hpp,
+    compiles and links with plain g++ (it is not run here: no GPU)."""
+    import subprocess
+    src = tmp_path / "driver.cpp"
+    src.write_text(DRIVER)
+    lib = library.LIB_PATH
+    r = subprocess.run(["g++", "-std=c++17", "-I", str(helpers.ROOT / "include"), str(src), "-o",
+                        str(tmp_path / "driver"), str(lib), "-Wl,-rpath," + str(lib.parent)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
