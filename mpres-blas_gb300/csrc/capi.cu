@@ -10,7 +10,6 @@
 #include <cstring>
 #include <map>
 #include <mutex>
-#include <string>
 #include <vector>
 
 #include "../../include/mpres_gb300.h"
@@ -26,19 +25,18 @@ using namespace mpres;
 
 namespace {
 
-thread_local std::string g_err;
+/* last error of this host thread; a fixed buffer, so reporting never allocates */
+thread_local char g_err[512];
 
 int fail(int code, const char *fmt, ...) {
-    char buf[512];
     va_list ap;
     va_start(ap, fmt);
-    vsnprintf(buf, sizeof(buf), fmt, ap);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
     va_end(ap);
-    g_err = buf;
     return code;
 }
 int ok() {
-    g_err.clear();
+    g_err[0] = '\0';
     return MPRES_SUCCESS;
 }
 int cuda_fail(cudaError_t e, const char *what) {
@@ -178,7 +176,7 @@ size_t mp_size(int nmod) { return 4 * (size_t)nmod + 40; }
 
 extern "C" {
 
-const char *mpres_last_error(void) { return g_err.c_str(); }
+const char *mpres_last_error(void) { return g_err; }
 
 size_t mpres_mp_float_size(int nmod) { return set_slot(nmod) < 0 ? 0 : mp_size(nmod); }
 
