@@ -136,6 +136,25 @@ int mpres_dot(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *
               mp_array_t *buffer, int gridDim1, int blockDim1, int gridDim2, int gridDim3, int blockDim3,
               void *stream);
 
+/* mp_dot that allocates nothing: no counterpart in the reference.  For callers
+ * that cannot allocate device memory once they are running -- a serving process
+ * that has reserved the whole device under a fixed memory budget, or a host
+ * application whose own allocator owns the GPU -- and for loops that cannot
+ * afford the device-wide synchronisation of cudaFree.  mpres_dot allocates a
+ * workspace on the first call on each stream; this variant keeps the gridDim3
+ * block sums in a static device array of MPRES_DOT_NOALLOC_MAX_BLOCKS entries
+ * (688 KB, held by every GPU that loads the library until the process exits)
+ * and rejects a larger gridDim3 with MPRES_ERR_INVALID_VALUE.  The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the one array: calls
+ * whose executions overlap on the GPU (other streams, other host threads) race
+ * and must be serialised by the caller.  The array needs no clearing: each call
+ * writes every block sum before it reads it.  Results are bit-identical to
+ * mpres_dot with the same gridDim3 and blockDim3. */
+#define MPRES_DOT_NOALLOC_MAX_BLOCKS 4096
+int mpres_dot_noalloc(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *y, int incy, mp_array_t *r,
+                      int gridDim3, int blockDim3, void *stream);
+
 /* cuda::mp_gemv<gridDim1, blockDim1, gridDim2, blockDim3> (src/blas/gemv.cuh:150-269):
  * y = alpha*op(A)*x + beta*y, A column-major.  blockDim3 fixes the summation order
  * (blockDim3 strided partial sums per row, then a tree).  buffer1/buffer2 are

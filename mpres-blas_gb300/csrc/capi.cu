@@ -376,6 +376,22 @@ int mpres_dot(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_dot");
 }
 
+int mpres_dot_noalloc(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *y, int incy, mp_array_t *r,
+                      int gridDim3, int blockDim3, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (n <= 0) return ok();
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dot_noalloc: null array");
+    if (gridDim3 <= 0 || gridDim3 > MPRES_DOT_NOALLOC_MAX_BLOCKS || blockDim3 <= 0 || blockDim3 > 1024)
+        return fail(MPRES_ERR_INVALID_VALUE,
+                    "mpres_dot_noalloc: gridDim3 %d must be in 1..%d and blockDim3 %d in 1..1024 (static scratch)",
+                    gridDim3, MPRES_DOT_NOALLOC_MAX_BLOCKS, blockDim3);
+    Workspace ws;
+    cudaError_t e = dot_noalloc_scratch(ws);
+    if (e != cudaSuccess) return cuda_fail(e, "mpres_dot_noalloc: scratch address");
+    e = launch_dot(nmod, n, *x, incx, *y, incy, *r, gridDim3, blockDim3, ws, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_dot_noalloc");
+}
+
 int mpres_gemv(int nmod, int trans, int m, int n, const mp_array_t *alpha, const mp_array_t *A, int lda,
                const mp_array_t *x, int incx, const mp_array_t *beta, mp_array_t *y, int incy, mp_array_t *buffer1,
                mp_array_t *buffer2, int gridDim1, int blockDim1, int gridDim2, int blockDim3, void *stream) {

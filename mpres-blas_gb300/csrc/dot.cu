@@ -17,6 +17,7 @@
  *   pass 2: one block of blockDim3 threads does the same over the gridDim3
  *           block sums and writes r[0].
  */
+#include "../../include/mpres_gb300.h"
 #include "kernels.h"
 #include "mp_device.cuh"
 
@@ -125,7 +126,31 @@ cudaError_t run(int n, const mp_array_t &x, int incx, const mp_array_t &y, int i
     return run_shape<N, 1024>(n, x, incx, y, incy, r, g3, b3, ws, s);
 }
 
+/* Scratch of mpres_dot_noalloc: the gridDim3 block sums of one call.  A
+ * file-scope device array, so that the entry point never allocates; every GPU
+ * that loads the library holds it until the process exits.  Its host-side name
+ * is a stand-in, not a device address: the address comes from
+ * cudaGetSymbolAddress, once per device, with that device current. */
+__device__ __align__(256) unsigned char g_dot_noalloc_scratch[MPRES_DOT_NOALLOC_MAX_BLOCKS * (4 * 32 + 40)];
+void *g_noalloc_addr[64];
+
 } // namespace
+
+cudaError_t dot_noalloc_scratch(Workspace &ws) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_dot_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    ws.ptr = g_noalloc_addr[dev];
+    ws.bytes = sizeof(g_dot_noalloc_scratch);
+    return cudaSuccess;
+}
 
 cudaError_t launch_dot(int nmod, int n, const mp_array_t &x, int incx, const mp_array_t &y, int incy,
                        const mp_array_t &r, int g3, int b3, Workspace ws, cudaStream_t s) {

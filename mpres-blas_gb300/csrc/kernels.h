@@ -28,6 +28,10 @@ struct Workspace {
 cudaError_t launch_dot(int nmod, int n, const mp_array_t &x, int incx, const mp_array_t &y, int incy,
                        const mp_array_t &r, int g3, int b3, Workspace ws, cudaStream_t s);
 
+/* address and size of the file-scope scratch of mpres_dot_noalloc on the current
+ * device (looked up once per device) */
+cudaError_t dot_noalloc_scratch(Workspace &ws);
+
 cudaError_t launch_gemv(int nmod, bool trans, int m, int n, const mp_array_t &alpha, const mp_array_t &A, int lda,
                         const mp_array_t &x, int incx, const mp_array_t &beta, const mp_array_t &y, int incy,
                         int b3, Workspace ws, cudaStream_t s);

@@ -59,6 +59,7 @@ _SIGS = {
     "mpres_ell_clear": (I, [P]),
     "mpres_set_d": (I, [I, P, SZ, P]),
     "mpres_dot": (I, [I, I, P, I, P, I, P, P, I, I, I, I, I, P]),
+    "mpres_dot_noalloc": (I, [I, I, P, I, P, I, P, I, I, P]),
     "mpres_gemv": (I, [I, I, I, I, P, P, I, P, I, P, P, I, P, P, I, I, I, I, P]),
     "mpres_gemm": (I, [I, I, I, I, I, I, P, P, I, P, I, P, P, I, P, I, I, I, I, I, P]),
     "mpres_spmv_csr": (I, [I, I, P, P, P, I, P]),
