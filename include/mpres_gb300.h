@@ -123,6 +123,18 @@ int mpres_ell_clear(ell_t *ell);
 /* mp_set_d (src/arith/assign.cuh:54-81), host: x[count] -> mp_float_t[count]. */
 int mpres_set_d(int nmod, const double *x, size_t count, void *out);
 
+/* The same conversion on the device, bit-identical to mpres_set_d (the
+ * reference's host mp_set_d with its host interval evaluation,
+ * src/rns.cuh:645-716); no counterpart in the reference, which converts on the
+ * host and copies with mp_array_host2device (src/mparray.cuh:76-118).
+ * x is a device array of count doubles.  mpres_set_d_device writes count AoS
+ * mp_float_t records to the device buffer out; mpres_array_set_d writes
+ * elements [offset, offset + count) of dst.  Both wait for the stream (they
+ * read back a flag: MPRES_ERR_NOT_SUPPORTED if an input would leave the replayed
+ * host behaviour, which no finite double is known to do). */
+int mpres_set_d_device(int nmod, const double *x, size_t count, void *out, void *stream);
+int mpres_array_set_d(int nmod, mp_array_t *dst, size_t offset, const double *x, size_t count, void *stream);
+
 /* ---- BLAS ---------------------------------------------------------------- */
 
 /* cuda::mp_dot<gridDim1, blockDim1, gridDim2, gridDim3, blockDim3>

@@ -25,6 +25,17 @@ int mpres_probe_dadd(int blocks, int threads, long long iters, void *sink, void 
  * (src/rns.cuh:848, :913); x and out are double[count] in device memory. */
 int mpres_probe_ceil_log2(const double *x, double *out, size_t count, void *stream);
 
+/* Self-checks of the exact replacements the kernels use for CUDA operations
+ * (each writes the replacement's result next to the CUDA operation's):
+ *   which 0: directed division by the set's RNS_EVAL_UNIT bounds, a = double[count],
+ *            out = double[4*count]: {div_rd, __ddiv_rd, div_ru, __ddiv_ru};
+ *   which 1: exponent-field scaling, a = double[count], b = int[count],
+ *            out = double[2*count]: {scale2(a, b), scalbn(a, b)};
+ *   which 2: ceil(log2) of fixed-point fractions, a = double[count] (multiples of
+ *            2^-83 below 1), out = int[2*count]: {from bits, ceil(log2(a))}.
+ * All pointers are device memory. */
+int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *out, size_t count, void *stream);
+
 /* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
  * element per thread: the device functions the BLAS kernels are built from,
  * exposed so that each can be checked against the reference on its own.

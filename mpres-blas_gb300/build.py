@@ -18,7 +18,8 @@ OUT = HERE / "_build"
 LIB = OUT / "libmpres_gb300.so"
 INCLUDE = HERE.parent / "include"
 
-CU_SOURCES = ["dot.cu", "gemv.cu", "gemm.cu", "spmv.cu", "capi.cu", "probe.cu", "elementwise.cu"]
+CU_SOURCES = ["dot.cu", "gemv.cu", "gemm.cu", "spmv.cu", "capi.cu", "probe.cu", "elementwise.cu", "convert.cu",
+              "batch.cu"]
 CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

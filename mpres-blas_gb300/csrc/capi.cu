@@ -5,6 +5,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -54,6 +55,10 @@ struct SetState {
 
 std::mutex g_mu;
 SetState g_sets[3];
+int *g_ceil_log2[64]; /* per device */
+int *g_host_log2[64];  /* per device: host_ceil_log2_table() */
+int g_host_log2_tab[2 * kHostLog2Entries];
+int g_host_log2_state = 0; /* 0 not measured, 1 measured, -1 the host's log2 is not usable */
 
 struct WsKey {
     int device;
@@ -62,7 +67,16 @@ struct WsKey {
 };
 std::map<WsKey, Workspace> g_ws;
 
-template <int N> void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, Tables<N> &t) {
+/* ceil(log2(2^e)) for e = -1074..1023 with CUDA's log2, the values the
+ * reference's refinement loop takes at exact powers of two (fixed_eval.cuh) */
+__global__ void ceil_log2_pow2_kernel(int *out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 2098) out[i] = (int)ceil(log2(ldexp(1.0, i - 1074)));
+}
+
+template <int N>
+void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, const int *dceil, const int *dhost_log2,
+                 Tables<N> &t) {
     std::memset(&t, 0, sizeof(t));
     for (int i = 0; i < N; i++) {
         t.moduli[i] = h.moduli[i];
@@ -86,16 +100,31 @@ template <int N> void fill_tables(const HostTables &h, const int *dpow2, const i
     t.inv_unit_upp = h.inv_unit_upp;
     t.pow2 = dpow2;
     t.pow2_inv = dpow2_inv;
+    t.ceil_log2_pow2 = dceil;
+    t.host_ceil_log2 = dhost_log2;
+    for (int i = 0; i < N; i++) t.recip_rn[i] = 1.0 / (double)h.moduli[i];
+    for (int i = 0; i < N; i++) {
+        t.recip_rd_m[i] = h.recip_rd_m[i];
+        t.recip_ru_m[i] = h.recip_ru_m[i];
+    }
+    t.eval_acc_fx[0] = h.eval_acc_fx[0];
+    t.eval_acc_fx[1] = h.eval_acc_fx[1];
+    t.unit_upp_recip = h.unit_upp_recip;
+    t.unit_low_recip = h.unit_low_recip;
 }
 
-template <int N> cudaError_t upload_all(const HostTables &h, const int *dpow2, const int *dpow2_inv) {
+template <int N>
+cudaError_t upload_all(const HostTables &h, const int *dpow2, const int *dpow2_inv, const int *dceil,
+                       const int *dhost_log2) {
     Tables<N> t;
-    fill_tables<N>(h, dpow2, dpow2_inv, t);
+    fill_tables<N>(h, dpow2, dpow2_inv, dceil, dhost_log2, t);
     cudaError_t e;
     if ((e = upload_tables_dot(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_gemv(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_gemm(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_elementwise(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_convert(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_batch(N, &t)) != cudaSuccess) return e;
     return upload_tables_spmv(N, &t);
 }
 
@@ -125,9 +154,22 @@ int init_locked(int nmod) {
         return cuda_fail(e, "cudaMemcpy(tables)");
     if ((e = cudaMemcpy(dinv, inv.data(), inv_bytes, cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(e, "cudaMemcpy(tables)");
-    if (nmod == 8) e = upload_all<8>(h, dpow2, dinv);
-    if (nmod == 16) e = upload_all<16>(h, dpow2, dinv);
-    if (nmod == 32) e = upload_all<32>(h, dpow2, dinv);
+    int *&dceil = g_ceil_log2[dev < 64 ? dev : 0];
+    if (!dceil) {
+        if ((e = cudaMalloc(&dceil, sizeof(int) * 2098)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+        ceil_log2_pow2_kernel<<<(2098 + 255) / 256, 256>>>(dceil);
+        if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail(e, "ceil_log2_pow2_kernel");
+    }
+    if (g_host_log2_state == 0) g_host_log2_state = host_ceil_log2_table(g_host_log2_tab) ? 1 : -1;
+    int *&dhl = g_host_log2[dev < 64 ? dev : 0];
+    if (!dhl && g_host_log2_state > 0) {
+        if ((e = cudaMalloc(&dhl, sizeof(g_host_log2_tab))) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+        if ((e = cudaMemcpy(dhl, g_host_log2_tab, sizeof(g_host_log2_tab), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemcpy(tables)");
+    }
+    if (nmod == 8) e = upload_all<8>(h, dpow2, dinv, dceil, dhl);
+    if (nmod == 16) e = upload_all<16>(h, dpow2, dinv, dceil, dhl);
+    if (nmod == 32) e = upload_all<32>(h, dpow2, dinv, dceil, dhl);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyToSymbol(tables)");
     st.device_tables[dev] = {dpow2, dinv};
     st.device_ready[dev] = true;
@@ -173,6 +215,20 @@ int workspace(cudaStream_t s, size_t bytes, Workspace &out) {
 size_t mp_size(int nmod) { return 4 * (size_t)nmod + 40; }
 
 } // namespace
+
+/* status reporting for the entry points of the other translation units */
+namespace mpres {
+int status_fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+int status_ok() { return ok(); }
+int status_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+int status_require(int nmod) { return require(nmod); }
+} // namespace mpres
 
 extern "C" {
 
@@ -360,6 +416,38 @@ int mpres_set_d(int nmod, const double *x, size_t count, void *out) {
     return ok();
 }
 
+/* the device conversion; out_aos or (dst, offset) */
+static int set_d_device(const char *what, int nmod, const double *x, size_t count, void *out_aos,
+                        const mp_array_t *dst, size_t offset, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count == 0) return ok();
+    if (!x || (!out_aos && !dst)) return fail(MPRES_ERR_INVALID_VALUE, "%s: null pointer", what);
+    if (g_host_log2_state < 0)
+        return fail(MPRES_ERR_NOT_SUPPORTED, "%s: the host log2 is not monotone near powers of two; use mpres_set_d",
+                    what);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, 256, ws)) return st;
+    int *flag = static_cast<int *>(ws.ptr);
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_set_d(nmod, x, (long long)count, out_aos, dst, (long long)offset, flag, s);
+    int h = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (h) return fail(MPRES_ERR_NOT_SUPPORTED, "%s: an input met a host-evaluation path not replayed on the device", what);
+    return ok();
+}
+
+int mpres_set_d_device(int nmod, const double *x, size_t count, void *out, void *stream) {
+    return set_d_device("mpres_set_d_device", nmod, x, count, out, nullptr, 0, stream);
+}
+
+int mpres_array_set_d(int nmod, mp_array_t *dst, size_t offset, const double *x, size_t count, void *stream) {
+    if (!dst) return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_set_d: null array");
+    return set_d_device("mpres_array_set_d", nmod, x, count, nullptr, dst, offset, stream);
+}
+
 int mpres_dot(int nmod, int n, const mp_array_t *x, int incx, const mp_array_t *y, int incy, mp_array_t *r,
               mp_array_t *buffer, int gridDim1, int blockDim1, int gridDim2, int gridDim3, int blockDim3,
               void *stream) {
@@ -437,7 +525,10 @@ int mpres_spmv_csr(int nmod, int m, const csr_t *csr, const void *x, void *y, in
     if (int st = require(nmod)) return st;
     if (m <= 0) return ok();
     if (!csr || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_csr: null argument");
-    cudaError_t e = launch_spmv_csr(nmod, m, *csr, x, y, static_cast<cudaStream_t>(stream));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, spmv_workspace_bytes(m), ws)) return st;
+    cudaError_t e = launch_spmv_csr(nmod, m, *csr, x, y, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_csr");
 }
 
@@ -450,7 +541,10 @@ int mpres_spmv_csrv(int nmod, int m, const csr_t *csr, const void *x, void *y, i
                     threadsPerRow);
     if (m <= 0) return ok();
     if (!csr || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_csrv: null argument");
-    cudaError_t e = launch_spmv_csrv(nmod, m, threadsPerRow, *csr, x, y, static_cast<cudaStream_t>(stream));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, spmv_workspace_bytes(m), ws)) return st;
+    cudaError_t e = launch_spmv_csrv(nmod, m, threadsPerRow, *csr, x, y, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_csrv");
 }
 
@@ -460,7 +554,10 @@ int mpres_spmv_ell(int nmod, int m, int maxnzr, const ell_t *ell, const void *x,
     if (int st = require(nmod)) return st;
     if (m <= 0) return ok();
     if (maxnzr < 0 || !ell || !x || !y) return fail(MPRES_ERR_INVALID_VALUE, "mpres_spmv_ell: bad argument");
-    cudaError_t e = launch_spmv_ell(nmod, m, maxnzr, *ell, x, y, static_cast<cudaStream_t>(stream));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, spmv_workspace_bytes(m), ws)) return st;
+    cudaError_t e = launch_spmv_ell(nmod, m, maxnzr, *ell, x, y, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_spmv_ell");
 }
 
@@ -472,6 +569,14 @@ int mpres_elementwise(int nmod, int op, const void *x, const void *y, void *r, s
     if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_elementwise: null pointer");
     cudaError_t e = launch_elementwise(nmod, op, x, y, r, (long long)count, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_elementwise");
+}
+
+int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *out, size_t count, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count == 0) return ok();
+    if (!a || !out || (which == 1 && !b)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_check: null pointer");
+    cudaError_t e = launch_check(which, nmod, a, b, out, (long long)count, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_check");
 }
 
 int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {

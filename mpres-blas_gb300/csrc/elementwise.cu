@@ -70,18 +70,16 @@ template <int N> __device__ __noinline__ void eval_full(er_t &low, er_t &upp, co
     const Tables<N> &t = T<N>();
     int s[N];
     for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
-    double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
-    if (!dnz(suml) && !dnz(sumu)) {
+    const fx sl = fx_fraction_sum<N, false>(s), su = fx_fraction_sum<N, true>(s);
+    if (fx_zero(sl) && fx_zero(su)) {
         low.frac = 0.0; low.exp = 0;
         upp.frac = 0.0; upp.exp = 0;
         return;
     }
-    const unsigned int whl = (unsigned int)suml, whu = (unsigned int)sumu;
-    suml = __dsub_rd(suml, (double)whl);
-    sumu = __dsub_ru(sumu, (double)whu);
-    er_set_d(low, suml);
-    er_set_d(upp, sumu);
+    const unsigned int whl = fx_whole(sl), whu = fx_whole(su);
+    const fx fl = fx_frac(sl), fu = fx_frac(su);
+    fx_er_set(low, fl);
+    fx_er_set(upp, fu);
     int mr = -1;
     if (whl != whu) mr = mrd<N>(x);
     if (mr > 0) {
@@ -89,8 +87,53 @@ template <int N> __device__ __noinline__ void eval_full(er_t &low, er_t &upp, co
         return;
     }
     if (mr == 0) low = t.unit_low;
-    if (sumu >= t.eval_acc) return;
-    eval_refine<N>(s, sumu, low, upp);
+    if (fx_ge_acc<N>(fu)) return;
+    eval_refine<N>(s, fu, low, upp);
+}
+
+/* self-checks of the replacements for CUDA operations (see the probe header) */
+template <int N>
+__global__ void check_div_kernel(const double *p, double *out, long long count) {
+    const Tables<N> &t = T<N>();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = p[i];
+        out[4 * i + 0] = div_by_const<false>(v, t.unit_upp.frac, t.unit_upp_recip);
+        out[4 * i + 1] = __ddiv_rd(v, t.unit_upp.frac);
+        out[4 * i + 2] = div_by_const<true>(v, t.unit_low.frac, t.unit_low_recip);
+        out[4 * i + 3] = __ddiv_ru(v, t.unit_low.frac);
+    }
+}
+
+__global__ void check_scale2_kernel(const double *x, const int *n, double *out, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        out[2 * i] = scale2(x[i], n[i]);
+        out[2 * i + 1] = scalbn(x[i], n[i]);
+    }
+}
+
+/* x must be F * 2^-83 with F < 2^83 holding at most 53 significant bits */
+template <int N>
+__global__ void check_ceil_log2_kernel(const double *x, int *out, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = x[i];
+        const uint64_t u = dbits(v);
+        const int e = (int)((u >> 52) & 2047) - 1023;
+        const uint64_t m = (u & ((1ull << 52) - 1)) | (1ull << 52); /* v = m * 2^(e-52) */
+        const int sh = e - 52 + kFixShift;                             /* F = m * 2^sh */
+        fx f;
+        if (sh >= 0) {
+            f.lo = sh >= 64 ? 0 : m << sh;
+            f.hi = sh == 0 ? 0 : (sh >= 64 ? m << (sh - 64) : m >> (64 - sh));
+        } else {
+            f.lo = m >> -sh;
+            f.hi = 0;
+        }
+        out[2 * i] = fx_ceil_log2<N>(f);
+        out[2 * i + 1] = (int)ceil(log2(v));
+    }
 }
 
 int blocks_for(long long count) {
@@ -132,6 +175,24 @@ cudaError_t launch_eval(int nmod, int fast, const int *digits, er_t *low, er_t *
     case 16: eval_op<16><<<g, 256, 0, s>>>(fast, digits, low, upp, count); break;
     case 32: eval_op<32><<<g, 256, 0, s>>>(fast, digits, low, upp, count); break;
     default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void *out, long long count,
+                         cudaStream_t s) {
+    const int g = blocks_for(count);
+    if (which == 0) {
+        if (nmod == 8) check_div_kernel<8><<<g, 256, 0, s>>>((const double *)a, (double *)out, count);
+        else if (nmod == 16) check_div_kernel<16><<<g, 256, 0, s>>>((const double *)a, (double *)out, count);
+        else if (nmod == 32) check_div_kernel<32><<<g, 256, 0, s>>>((const double *)a, (double *)out, count);
+        else return cudaErrorInvalidValue;
+    } else if (which == 1) {
+        check_scale2_kernel<<<g, 256, 0, s>>>((const double *)a, (const int *)b, (double *)out, count);
+    } else if (which == 2) {
+        check_ceil_log2_kernel<8><<<g, 256, 0, s>>>((const double *)a, (int *)out, count);
+    } else {
+        return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }

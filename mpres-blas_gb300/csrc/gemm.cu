@@ -14,6 +14,9 @@
  * arithmetic, so the buffer matrix never leaves registers.  The k chain keeps
  * the reference's order (no split-k), so results are bit-identical.
  */
+/* every SM holds many product chains here and the FP64 pipe binds: the
+ * interval evaluation runs in fixed point on the integer pipes (mp_device.cuh) */
+#define MPRES_EVAL_FIXED_POINT 1
 #include "kernels.h"
 #include "mp_device.cuh"
 

@@ -163,6 +163,32 @@ void set_d(const HostTables &t, double x, char *out) {
 
 } // namespace
 
+/* How ceil(std::log2(x)) -- the call of the refinement loop above -- behaves just
+ * above each power of two 2^e, e = -1022..0.  out[2(e+1022)] = ceil(log2(2^e));
+ * out[2(e+1022)+1] = the smallest j >= 1 with ceil(log2(2^e (1 + j 2^-52))) =
+ * e + 1 (below it the rounded logarithm is still e).  Further from 2^e the
+ * logarithm is at least one unit of its last place above e, so every log2
+ * within one ulp gives the exact ceiling.  Returns false if the host's log2 is
+ * not monotone over the probed window. */
+bool host_ceil_log2_table(int *out) {
+    for (int e = -1022; e <= 0; e++) {
+        const double p = std::ldexp(1.0, e);
+        out[2 * (e + 1022)] = (int)std::ceil(std::log2(p));
+        int thr = 0;
+        for (int j = 1; j < (1 << 20); j++) {
+            const double x = p + std::ldexp((double)j, e - 52);
+            const int c = (int)std::ceil(std::log2(x));
+            if (c == e + 1) { thr = j; break; }
+            if (c != e) return false;
+        }
+        if (thr == 0) return false;
+        for (int j = thr; j < thr + 256; j++)
+            if ((int)std::ceil(std::log2(p + std::ldexp((double)j, e - 52))) != e + 1) return false;
+        out[2 * (e + 1022) + 1] = thr;
+    }
+    return true;
+}
+
 void host_set_d(const HostTables &t, const double *x, size_t count, void *out) {
     const size_t stride = 4 * (size_t)t.n + 40;
     char *o = static_cast<char *>(out);

@@ -67,6 +67,44 @@ int product_words(const int *moduli, int n, uint32_t *w) {
     return len;
 }
 
+/* v = M * 2^shift with M the 53-bit significand of v as an integer (v > 0);
+ * false unless the shift lands in [0, 10] */
+bool mantissa_at(double v, int shift, uint64_t &M) {
+    int e;
+    const double f = std::frexp(v, &e); /* v = f * 2^e, f in [0.5, 1) */
+    const uint64_t m = (uint64_t)std::ldexp(f, 53);
+    const int s = e - 53 - shift;       /* v = m * 2^(e-53) = (m << s) * 2^shift */
+    if (s < 0 || s > 10) return false;
+    M = m << s;
+    return true;
+}
+
+/* the integer forms the fixed-point evaluation uses (every recip is R * 2^-83
+ * with a 53-bit R; eval_acc as the 128-bit ceiling of eval_acc * 2^83); false
+ * if a constant is outside that range */
+bool compute_fixed_forms(HostTables &t) {
+    for (int i = 0; i < t.n; i++) {
+        int e;
+        std::frexp(t.recip_rd[i], &e);
+        if (e != -30 || !mantissa_at(t.recip_rd[i], -83, t.recip_rd_m[i])) return false;
+        std::frexp(t.recip_ru[i], &e);
+        if (e != -30 || !mantissa_at(t.recip_ru[i], -83, t.recip_ru_m[i])) return false;
+        if (t.recip_rd_m[i] >= (1ull << 53) || t.recip_ru_m[i] >= (1ull << 53)) return false;
+    }
+    int e;
+    const uint64_t m = (uint64_t)std::ldexp(std::frexp(t.eval_acc, &e), 53); /* eval_acc = m * 2^(e-53) */
+    const int s = e - 53 + 83;
+    if (!(t.eval_acc > 0) || s > 64 || s < -63) return false;
+    const unsigned __int128 acc =
+        s >= 0 ? (unsigned __int128)m << s : ((unsigned __int128)m + ((1ull << -s) - 1)) >> -s;
+    t.eval_acc_fx[0] = (uint64_t)acc;
+    t.eval_acc_fx[1] = (uint64_t)(acc >> 64);
+    if (!(t.unit_upp.frac > 0) || !(t.unit_low.frac > 0)) return false;
+    t.unit_upp_recip = 1.0 / t.unit_upp.frac;
+    t.unit_low_recip = 1.0 / t.unit_low.frac;
+    return true;
+}
+
 } // namespace
 
 bool compute_host_tables(int n, HostTables &t) {
@@ -152,7 +190,7 @@ bool compute_host_tables(int n, HostTables &t) {
     t.mp_precision = E / 2 - 1;
     t.mp_h = (E % 2 == 0) ? -(E / 2) - 1 : -((E + 1) / 2);
     t.mp_j = -1;
-    return true;
+    return compute_fixed_forms(t);
 }
 
 } // namespace mpres

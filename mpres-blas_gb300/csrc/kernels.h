@@ -17,6 +17,8 @@ cudaError_t upload_tables_gemv(int n, const void *tab);
 cudaError_t upload_tables_gemm(int n, const void *tab);
 cudaError_t upload_tables_spmv(int n, const void *tab);
 cudaError_t upload_tables_elementwise(int n, const void *tab);
+cudaError_t upload_tables_convert(int n, const void *tab);
+cudaError_t upload_tables_batch(int n, const void *tab);
 
 /* Scratch for one call, carved from a per-device workspace. */
 struct Workspace {
@@ -40,16 +42,35 @@ cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, 
                         const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
                         cudaStream_t s);
 
-cudaError_t launch_spmv_csr(int nmod, int m, const csr_t &csr, const void *x, void *y, cudaStream_t s);
-cudaError_t launch_spmv_csrv(int nmod, int m, int tpr, const csr_t &csr, const void *x, void *y, cudaStream_t s);
-cudaError_t launch_spmv_ell(int nmod, int m, int maxnzr, const ell_t &ell, const void *x, void *y, cudaStream_t s);
+/* SpMV: the row schedule (length-sorted order) goes to ws */
+size_t spmv_workspace_bytes(int m);
+cudaError_t launch_spmv_csr(int nmod, int m, const csr_t &csr, const void *x, void *y, Workspace ws, cudaStream_t s);
+cudaError_t launch_spmv_csrv(int nmod, int m, int tpr, const csr_t &csr, const void *x, void *y, Workspace ws,
+                             cudaStream_t s);
+cudaError_t launch_spmv_ell(int nmod, int m, int maxnzr, const ell_t &ell, const void *x, void *y, Workspace ws,
+                            cudaStream_t s);
+
+/* double -> mp_float_t on the device (host mp_set_d semantics): into AoS
+ * out_aos when non-null, else into elements [offset, offset + count) of out_soa;
+ * *flag |= 1 if an input took a path outside the replayed host behaviour */
+cudaError_t launch_set_d(int nmod, const double *x, long long count, void *out_aos, const mp_array_t *out_soa,
+                         long long offset, int *flag, cudaStream_t s);
 
 cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, void *r, long long count,
                                cudaStream_t s);
 cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,
                              cudaStream_t s);
+cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void *out, long long count,
+                         cudaStream_t s);
 cudaError_t launch_eval(int nmod, int fast, const int *digits, er_t *low, er_t *upp, long long count,
                         cudaStream_t s);
+
+/* status reporting shared by the C entry points (capi.cu): set the thread's
+ * last-error text and return the status */
+int status_fail(int code, const char *fmt, ...);
+int status_ok();
+int status_cuda(cudaError_t e, const char *what);
+int status_require(int nmod); /* MPRES_SUCCESS if mpres_init(nmod) ran on the current device */
 
 } // namespace mpres
 

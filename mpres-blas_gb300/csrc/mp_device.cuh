@@ -114,6 +114,17 @@ __device__ __forceinline__ void er_set_d(er_t &r, double x) {
     }
 }
 
+/* scalbn(x, n): for a normal x whose result stays normal, adding n to the
+ * exponent field is the exact result; other cases (zero, subnormal, overflow)
+ * go to CUDA's scalbn, which the reference calls in every case. */
+__device__ __forceinline__ double scale2(double x, int n) {
+    const uint64_t u = dbits(x);
+    const int e = (int)((u >> 52) & 2047);
+    if (e != 0 && e != 2047 && e + n >= 1 && e + n <= 2046)
+        return bdbl(u + ((uint64_t)(int64_t)n << 52));
+    return scalbn(x, n);
+}
+
 /* er_add_rd / er_add_ru, src/extrange.cuh:451-490 */
 template <bool UP> __device__ __forceinline__ er_t er_add(er_t x, er_t y) {
     const bool xnz = dnz(x.frac), ynz = dnz(y.frac);
@@ -123,10 +134,10 @@ template <bool UP> __device__ __forceinline__ er_t er_add(er_t x, er_t y) {
     er_t r;
     if (dexp > 0) {
         r.exp = x.exp;
-        r.frac = dadd<UP>(x.frac, scalbn(y.frac, (int)-dexp));
+        r.frac = dadd<UP>(x.frac, scale2(y.frac, (int)-dexp));
     } else if (dexp < 0) {
         r.exp = y.exp;
-        r.frac = dadd<UP>(y.frac, scalbn(x.frac, (int)dexp));
+        r.frac = dadd<UP>(y.frac, scale2(x.frac, (int)dexp));
     } else {
         r.exp = (x.exp == 0) ? y.exp : x.exp;
         r.frac = dadd<UP>(x.frac, y.frac);
@@ -135,11 +146,62 @@ template <bool UP> __device__ __forceinline__ er_t er_add(er_t x, er_t y) {
     return r;
 }
 
-/* er_md_rd / er_md_ru (x*y/z), src/extrange.cuh:627-644 */
-template <bool UP> __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z) {
+/* Directed division p / z by a positive constant z with zr = RN(1/z): the
+ * classical quotient correction.  q0 = RN(p * zr) is within two ulps of p/z; the
+ * sign of the remainder p - q*z, obtained exactly from one FMA (it is rounded
+ * once, and a nonzero remainder of this size cannot round to zero), decides
+ * whether q*z lies below or above p, so stepping q by ulps until the sign flips
+ * gives the correctly rounded quotient in the requested direction -- the value
+ * __ddiv_rd / __ddiv_ru return.  Inputs outside the normal range where those
+ * bounds hold are passed to the intrinsics. */
+__device__ __forceinline__ double next_up(double q) {
+    const int64_t u = (int64_t)dbits(q);
+    if (u == 0 || u == (int64_t)kSign) return bdbl(1); /* +-0 -> smallest subnormal */
+    return bdbl((uint64_t)(u >= 0 ? u + 1 : u - 1));
+}
+__device__ __forceinline__ double next_down(double q) { return -next_up(-q); }
+
+template <bool UP> __device__ __forceinline__ double div_by_const(double p, double z, double zr) {
+    const uint64_t ep = (dbits(p) >> 52) & 2047;
+    if (ep < 64 || ep > 1984) return ddiv<UP>(p, z); /* zero, subnormal, huge: exact intrinsic */
+    double q = __dmul_rn(p, zr);
+    if (!UP) {
+        /* largest q with q*z <= p */
+        if (__fma_rn(-q, z, p) < 0.0) {
+            q = next_down(q);
+            if (__fma_rn(-q, z, p) < 0.0) q = next_down(q);
+        } else {
+            double qn = next_up(q);
+            if (__fma_rn(-qn, z, p) >= 0.0) {
+                q = qn;
+                qn = next_up(q);
+                if (__fma_rn(-qn, z, p) >= 0.0) q = qn;
+            }
+        }
+    } else {
+        /* smallest q with q*z >= p */
+        if (__fma_rn(-q, z, p) > 0.0) {
+            q = next_up(q);
+            if (__fma_rn(-q, z, p) > 0.0) q = next_up(q);
+        } else {
+            double qn = next_down(q);
+            if (__fma_rn(-qn, z, p) <= 0.0) {
+                q = qn;
+                qn = next_down(q);
+                if (__fma_rn(-qn, z, p) <= 0.0) q = qn;
+            }
+        }
+    }
+    return q;
+}
+
+/* er_md_rd / er_md_ru (x*y/z), src/extrange.cuh:627-644; z is RNS_EVAL_UNIT's
+ * upper (RD) or lower (RU) bound and zr the nearest double to its reciprocal */
+template <bool UP>
+__device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z, double zr) {
     er_t r;
     r.exp = x.exp + y.exp - z.exp;
-    r.frac = ddiv<UP>(dmul<UP>(x.frac, y.frac), z.frac);
+    r.frac = div_by_const<UP>(dmul<UP>(x.frac, y.frac), z.frac, zr);
     er_adjust(r);
     return r;
 }
@@ -168,6 +230,14 @@ template <int N, bool UP, class F> __device__ __forceinline__ double psum(const 
     static_assert(N >= 4, "moduli sets have at least 4 moduli");
     return psum_node<psum_span(N), N, UP>(leaf, 0);
 }
+
+} // namespace dev
+} // namespace mpres
+
+#include "fixed_eval.cuh"
+
+namespace mpres {
+namespace dev {
 
 /* --------------------------- RNS algorithms ------------------------------ */
 
@@ -218,7 +288,23 @@ template <int N> __device__ __forceinline__ int pow2_row_index(int r) {
     return r > T<N>().log2m ? T<N>().log2m : r;
 }
 
-/* Refinement loop of rns_eval_compute[_fast], src/rns.cuh:843-867 / :908-932 */
+/* The interval evaluation and the rank come in two forms with identical
+ * results: on the FP64 pipe, as the reference computes them (directed-rounding
+ * products and pairwise sums), and in fixed point on the integer pipes
+ * (fixed_eval.cuh).  The fixed-point form issues about twice the instructions
+ * and makes a longer dependency chain, but takes the work off the FP64 pipe,
+ * GB300's narrowest.  Measured on GB300: fixed point is 5% faster in mp_gemm
+ * (32 moduli, every SM full of warps, FP64 pipe bound) and slower everywhere
+ * else -- 2.4x slower in mp_gemv, 3x in mp_dot's reduction -- where few warps
+ * per SM make latency and instruction fetch bind.  A translation unit picks one
+ * with MPRES_EVAL_FIXED_POINT (0 = FP64, the default) before including this
+ * header. */
+#ifndef MPRES_EVAL_FIXED_POINT
+#define MPRES_EVAL_FIXED_POINT 0
+#endif
+
+/* Refinement loop of rns_eval_compute[_fast], src/rns.cuh:843-867 / :908-932,
+ * on the FP64 pipe: sumu is the current upper fraction, below RNS_EVAL_ACCURACY */
 template <int N>
 __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &upp) {
     const Tables<N> &t = T<N>();
@@ -242,12 +328,40 @@ __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &u
     upp.exp -= K;
 }
 
+/* the same loop in fixed point: fu is the current upper fraction */
+template <int N>
+__device__ __noinline__ void eval_refine(int *s, fx fu, er_t &low, er_t &upp) {
+    const Tables<N> &t = T<N>();
+    int K = 0;
+    for (int guard = 0; !fx_ge_acc<N>(fu) && guard < 4096; guard++) {
+        int k;
+        if (fx_zero(fu)) {
+            k = t.log2m; /* log2(0): the reference's index saturates past the table */
+        } else {
+            const int c = fx_ceil_log2<N>(fu);
+            k = -(c + 1) > t.ref_factor ? -(c + 1) : t.ref_factor;
+            k = pow2_row_index<N>(k);
+        }
+        const int *row = t.pow2 + (size_t)k * N;
+#pragma unroll
+        for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
+        fu = fx_frac(fx_fraction_sum<N, true>(s));
+        K += k;
+    }
+    const fx fl = fx_frac(fx_fraction_sum<N, false>(s));
+    fx_er_set(low, fl);
+    fx_er_set(upp, fu);
+    low.exp -= K;
+    upp.exp -= K;
+}
+
 /* cuda::rns_eval_compute_fast, src/rns.cuh:878-933 */
 template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp, const int *x) {
     const Tables<N> &t = T<N>();
     int s[N];
 #pragma unroll
     for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
+#if !MPRES_EVAL_FIXED_POINT
     double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
     double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
     if (!dnz(suml) && !dnz(sumu)) {
@@ -263,21 +377,45 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
         return;
     }
     eval_refine<N>(s, sumu, low, upp);
+#else
+    const fx sl = fx_fraction_sum<N, false>(s);
+    const fx su = fx_fraction_sum<N, true>(s);
+    if (fx_zero(sl) && fx_zero(su)) {
+        low.frac = 0.0; low.exp = 0;
+        upp.frac = 0.0; upp.exp = 0;
+        return;
+    }
+    const fx fl = fx_frac(sl), fu = fx_frac(su);
+    if (fx_ge_acc<N>(fu)) {
+        fx_er_set(low, fl);
+        fx_er_set(upp, fu);
+        return;
+    }
+    eval_refine<N>(s, fu, low, upp);
+#endif
 }
 
 /* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */
 template <int N> __device__ __forceinline__ int rank_full(const int *x, const int *s) {
+#if MPRES_EVAL_FIXED_POINT
+    const unsigned int whl = fx_whole(fx_fraction_sum<N, false>(s));
+    const unsigned int whu = fx_whole(fx_fraction_sum<N, true>(s));
+#else
     const Tables<N> &t = T<N>();
-    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
-    double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
-    unsigned int whl = (unsigned int)suml, whu = (unsigned int)sumu;
+    const unsigned int whl = (unsigned int)psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
+    const unsigned int whu = (unsigned int)psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+#endif
     if (whl == whu) return (int)whl;
     return (mrd<N>(x) == 0) ? (int)whu : (int)whl;
 }
 /* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096 */
 template <int N> __device__ __forceinline__ int rank_fast(const int *s) {
+#if MPRES_EVAL_FIXED_POINT
+    return (int)fx_whole(fx_fraction_sum<N, true>(s));
+#else
     const Tables<N> &t = T<N>();
     return (int)psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+#endif
 }
 
 /* cuda::make_scaling_step, src/rns.cuh:1101-1124, for 1 <= j <= 30.  Residues
@@ -437,8 +575,8 @@ template <int N> __device__ __forceinline__ void mp_mul(mp_t<N> &r, const mp_t<N
     const Tables<N> &t = T<N>();
     r.exp = x.exp + y.exp;
     r.sign = x.sign ^ y.sign;
-    r.ev[0] = er_md<false>(x.ev[0], y.ev[0], t.unit_upp);
-    r.ev[1] = er_md<true>(x.ev[1], y.ev[1], t.unit_low);
+    r.ev[0] = er_md<false>(x.ev[0], y.ev[0], t.unit_upp, t.unit_upp_recip);
+    r.ev[1] = er_md<true>(x.ev[1], y.ev[1], t.unit_low, t.unit_low_recip);
 #pragma unroll
     for (int i = 0; i < N; i++) r.d[i] = mulmod_i<N>(x.d[i], y.d[i], i);
     round_if_needed<N>(r);

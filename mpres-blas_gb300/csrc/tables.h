@@ -39,6 +39,16 @@ struct Tables {
     er_t inv_unit_low, inv_unit_upp; /* RNS_EVAL_INV_UNIT */
     const int *pow2;     /* device: RNS_POW2[(log2m + 1)][N], 2^r mod m_i */
     const int *pow2_inv; /* device: RNS_POW2_INVERSE[30][N], (2^(r+1))^-1 mod m_i */
+    /* integer forms for the fixed-point evaluation (fixed_eval.cuh) */
+    uint64_t recip_rd_m[N];      /* RNS_MODULI_RECIP_RD[i] = recip_rd_m[i] * 2^-83 */
+    uint64_t recip_ru_m[N];      /* RNS_MODULI_RECIP_RU[i] = recip_ru_m[i] * 2^-83 */
+    uint64_t eval_acc_fx[2];     /* ceil(RNS_EVAL_ACCURACY * 2^83) as {low, high} 64-bit words */
+    double unit_upp_recip;       /* nearest double to 1 / RNS_EVAL_UNIT.upp.frac */
+    double unit_low_recip;       /* nearest double to 1 / RNS_EVAL_UNIT.low.frac */
+    const int *ceil_log2_pow2;   /* device: ceil(log2(2^e)) by CUDA's log2, e = -1074..1023 */
+    /* the host conversion (double -> mp_float_t) replayed on the device */
+    double recip_rn[N];          /* 1.0 / m_i rounded to nearest, as the host computes it */
+    const int *host_ceil_log2;   /* device: host_ceil_log2_table() */
 };
 
 /* Host-side copy of every table in the reference's array shapes. */
@@ -56,11 +66,18 @@ struct HostTables {
     int ref_factor = 0, mp_h = 0, mp_j = 0, mp_precision = 0;
     er_t unit_low, unit_upp, inv_unit_low, inv_unit_upp;
     int *pow2 = nullptr; /* host, (log2m + 1) * n */
+    uint64_t recip_rd_m[32], recip_ru_m[32], eval_acc_fx[2]; /* the Tables<N> integer forms */
+    double unit_upp_recip = 0, unit_low_recip = 0;
 };
 
 /* Computes every table of the predefined set of n moduli (n in {8, 16, 32});
  * returns false for other sizes. */
 bool compute_host_tables(int n, HostTables &t);
+
+/* ceil(std::log2(x)) of the host just above powers of two (host_convert.cpp);
+ * 2 * kHostLog2Entries ints */
+constexpr int kHostLog2Entries = 1023;
+bool host_ceil_log2_table(int *out);
 
 } // namespace mpres
 

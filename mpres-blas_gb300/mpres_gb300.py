@@ -58,6 +58,8 @@ _SIGS = {
     "mpres_ell_host2device": (I, [P, P, I, I]),
     "mpres_ell_clear": (I, [P]),
     "mpres_set_d": (I, [I, P, SZ, P]),
+    "mpres_set_d_device": (I, [I, P, SZ, P, P]),
+    "mpres_array_set_d": (I, [I, P, SZ, P, SZ, P]),
     "mpres_dot": (I, [I, I, P, I, P, I, P, P, I, I, I, I, I, P]),
     "mpres_dot_noalloc": (I, [I, I, P, I, P, I, P, I, I, P]),
     "mpres_gemv": (I, [I, I, I, I, P, P, I, P, I, P, P, I, P, P, I, I, I, I, P]),
@@ -65,10 +67,19 @@ _SIGS = {
     "mpres_spmv_csr": (I, [I, I, P, P, P, I, P]),
     "mpres_spmv_csrv": (I, [I, I, P, P, P, I, I, P]),
     "mpres_spmv_ell": (I, [I, I, I, P, P, P, I, P]),
+    "mpres_batch_create": (I, [I, P]),
+    "mpres_batch_destroy": (I, [P]),
+    "mpres_batch_add_gemv": (I, [P, I, I, I, P, P, I, P, I, P, P, I, I]),
+    "mpres_batch_add_dot": (I, [P, I, P, I, P, I, P, I, I]),
+    "mpres_batch_add_spmv_csr": (I, [P, I, P, P, P]),
+    "mpres_batch_commit": (I, [P, ctypes.c_uint, P]),
+    "mpres_batch_run": (I, [P, P]),
+    "mpres_batch_info": (I, [P, P]),
     "mpres_probe_mulmod": (I, [I, I, ctypes.c_longlong, P, P]),
     "mpres_probe_dadd": (I, [I, I, ctypes.c_longlong, P, P]),
     "mpres_elementwise": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_ceil_log2": (I, [P, P, SZ, P]),
+    "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
     "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
 }
@@ -113,6 +124,28 @@ def set_d(nmod, x):
     out = np.zeros(x.size, mp_dtype(nmod))
     check(lib().mpres_set_d(nmod, x.ctypes.data, x.size, out.ctypes.data), "mpres_set_d")
     return out
+
+
+def set_d_device(nmod, x, out=None, stream=None):
+    """Device conversion (bit-identical to set_d) of a float64 torch CUDA tensor
+    into AoS records; returns the DeviceBytes it wrote."""
+    n = x.numel()
+    out = out if out is not None else DeviceBytes(n * mp_size(nmod))
+    check(lib().mpres_set_d_device(nmod, x.data_ptr(), n, out.ptr, _stream_handle(stream)), "mpres_set_d_device")
+    return out
+
+
+def array_set_d(nmod, arr, offset, x, stream=None):
+    """Device conversion of a float64 torch CUDA tensor into elements
+    [offset, offset + x.numel()) of a DeviceArray."""
+    if offset < 0 or offset + x.numel() > arr.size:
+        raise MpresError("array_set_d: elements [%d, %d) outside an array of %d" % (offset, offset + x.numel(), arr.size))
+    check(lib().mpres_array_set_d(nmod, arr.ref, offset, x.data_ptr(), x.numel(), _stream_handle(stream)),
+          "mpres_array_set_d")
+
+
+def mp_size(nmod):
+    return 4 * nmod + 40
 
 
 def _stream_handle(stream):
@@ -269,6 +302,57 @@ def spmv_ell(nmod, m, ell, x, y, threads=32, stream=None):
                                _stream_handle(stream)), "mpres_spmv_ell")
 
 
+BATCH_GRAPH, BATCH_AUTOTUNE = 1, 2
+
+
+class Batch:
+    """A batch of mp_gemv / mp_dot / mp_spmv_csr operations run as one persistent
+    launch (include/mpres_gb300_batch.h).  Operands must outlive the batch."""
+
+    def __init__(self, nmod):
+        self.nmod = nmod
+        self.h = ctypes.c_void_p()
+        check(lib().mpres_batch_create(nmod, ctypes.byref(self.h)), "mpres_batch_create")
+        self._keep = []
+
+    def add_gemv(self, trans, m, n, alpha, A, lda, x, beta, y, incx=1, incy=1, b3=32):
+        self._keep += [alpha, A, x, beta, y]
+        check(lib().mpres_batch_add_gemv(self.h, trans, m, n, alpha.ref, A.ref, lda, x.ref, incx, beta.ref, y.ref,
+                                         incy, b3), "mpres_batch_add_gemv")
+
+    def add_dot(self, n, x, y, r, incx=1, incy=1, g3=256, b3=64):
+        self._keep += [x, y, r]
+        check(lib().mpres_batch_add_dot(self.h, n, x.ref, incx, y.ref, incy, r.ref, g3, b3), "mpres_batch_add_dot")
+
+    def add_spmv_csr(self, m, csr, x, y):
+        self._keep += [csr, x, y]
+        check(lib().mpres_batch_add_spmv_csr(self.h, m, ctypes.byref(csr.c), x.ptr, y.ptr),
+              "mpres_batch_add_spmv_csr")
+
+    def commit(self, flags=BATCH_GRAPH, stream=None):
+        check(lib().mpres_batch_commit(self.h, flags, _stream_handle(stream)), "mpres_batch_commit")
+
+    def run(self, stream=None):
+        check(lib().mpres_batch_run(self.h, _stream_handle(stream)), "mpres_batch_run")
+
+    def info(self):
+        out = (ctypes.c_longlong * 8)()
+        check(lib().mpres_batch_info(self.h, out), "mpres_batch_info")
+        keys = ("ops", "tasks", "threads", "ctas", "graph", "autotuned", "scratch_bytes", "candidates")
+        return dict(zip(keys, list(out)))
+
+    def destroy(self):
+        if self.h:
+            check(lib().mpres_batch_destroy(self.h), "mpres_batch_destroy")
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 OP_ADD, OP_MUL, OP_MUL_D = 0, 1, 2
 
 
@@ -311,3 +395,17 @@ def probe_ceil_log2(x):
     check(lib().mpres_probe_ceil_log2(dx.ptr, do.ptr, x.size, None), "mpres_probe_ceil_log2")
     torch.cuda.synchronize()
     return do.to_numpy(np.float64, x.size)
+
+
+def probe_check(which, nmod, a, b=None):
+    """Runs a replacement self-check (see mpres_gb300_probe.h) and returns its output pairs."""
+    import torch
+    a = np.ascontiguousarray(a)
+    da = DeviceBytes.from_numpy(a)
+    db = DeviceBytes.from_numpy(np.ascontiguousarray(b)) if b is not None else None
+    width, dt = {0: (4, np.float64), 1: (2, np.float64), 2: (2, np.int32)}[which]
+    out = DeviceBytes(len(a) * width * np.dtype(dt).itemsize)
+    check(lib().mpres_probe_check(which, nmod, da.ptr, db.ptr if db else None, out.ptr, len(a), None),
+          "mpres_probe_check")
+    torch.cuda.synchronize()
+    return out.to_numpy(dt, len(a) * width).reshape(len(a), width)

@@ -535,8 +535,16 @@ static void eval_refine(const ora_ctx_t *c, int *s, double sumu, er_t *low, er_t
     double fracl[ORA_MAXN], fracu[ORA_MAXN];
     int K = 0;
     while (sumu < c->eval_acc) {
-        double a = -(dev_ceil_log2(sumu) + 1);
-        int k = (int)(a > c->ref_factor ? a : c->ref_factor);
+        int k;
+        if (sumu == 0) {
+            /* log2(0) = -inf: the reference's row index saturates past RNS_POW2; the
+             * library clamps it to the last row, and so does the oracle */
+            k = c->log2m;
+        } else {
+            double a = -(dev_ceil_log2(sumu) + 1);
+            k = (int)(a > c->ref_factor ? a : c->ref_factor);
+            if (k > c->log2m) k = c->log2m;
+        }
         rns_mul(c, s, s, &c->pow2[k * n]);
         for (int i = 0; i < n; i++) fracu[i] = mul_ru(s[i], c->recip_ru[i]);
         sumu = psum(fracu, n, add_ru);

@@ -71,3 +71,59 @@ def test_eval_vs_oracle(gpu, oracle, n, fast):
         lo1, up1 = gpu.rns_eval(n, digits, fast)
         lo2, up2 = (oracle.eval_fast if fast else oracle.eval)(n, digits)
         assert lo1.tobytes() == lo2.tobytes() and up1.tobytes() == up2.tobytes()
+
+
+def _doubles_all_binades(rng, count):
+    """Random doubles over every exponent and both signs, plus edge values."""
+    bits = rng.integers(0, 1 << 63, count, dtype=np.int64).astype(np.uint64)
+    bits |= rng.integers(0, 2, count).astype(np.uint64) << np.uint64(63)
+    x = bits.view(np.float64)
+    x = x[np.isfinite(x)]
+    edge = np.array([0.0, -0.0, 1.0, -1.0, 2.0, 0.5, np.nextafter(1.0, 2.0), np.nextafter(2.0, 0.0), 5e-324,
+                     2.0 ** -1022, np.finfo(float).max, -np.finfo(float).max, 3.9999999999999996, 1.0000000000000002])
+    return np.concatenate([edge, x])
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_directed_division_matches_cuda(gpu, n):
+    """er_md's division by the constant RNS_EVAL_UNIT bound (one multiply and FMA
+    remainder sign tests) gives the bits of __ddiv_rd / __ddiv_ru."""
+    rng = np.random.default_rng(helpers.SEED + 930 + n)
+    # the operands er_md sees: products of two significands in [1, 2) (and [0.5, 1)), rounded
+    a, b = rng.uniform(1, 2, 400000), rng.uniform(0.5, 2, 400000)
+    p = np.concatenate([a * b, np.nextafter(a * b, 0), np.nextafter(a * b, 4), _doubles_all_binades(rng, 400000)])
+    out = gpu.probe_check(0, n, p)
+    v = out.view(np.int64)
+    assert (v[:, 0] == v[:, 1]).all(), p[v[:, 0] != v[:, 1]][:5]
+    assert (v[:, 2] == v[:, 3]).all(), p[v[:, 2] != v[:, 3]][:5]
+
+
+def test_exponent_scaling_matches_scalbn(gpu):
+    rng = np.random.default_rng(helpers.SEED + 940)
+    x = _doubles_all_binades(rng, 300000)
+    k = rng.integers(-2200, 2200, len(x)).astype(np.int32)
+    k[: len(x) // 2] = rng.integers(-600, 0, len(x) // 2)  # the er_add range: shifts down
+    out = gpu.probe_check(1, 8, x, k).view(np.int64)
+    assert (out[:, 0] == out[:, 1]).all()
+
+
+def test_fixed_point_ceil_log2_matches_cuda(gpu):
+    """ceil(log2(x)) from the bits of a fixed-point fraction (with CUDA's log2 at and
+    near powers of two) equals ceil(log2(x)) computed with CUDA's log2."""
+    rng = np.random.default_rng(helpers.SEED + 950)
+    vals = []
+    for k in range(0, 83):  # x = F * 2^-83 with F near 2^k
+        step = 1 << max(0, k - 52)
+        for j in range(-3000, 3001, 1 if k < 20 else 7):
+            F = (1 << k) + j * step
+            if 0 < F < (1 << 83):
+                vals.append(F)
+    for _ in range(200000):  # random fractions with at most 53 significant bits
+        L = int(rng.integers(1, 84))
+        F = int(rng.integers(1 << (L - 1), 1 << L)) if L < 63 else int(rng.integers(1 << 52, 1 << 53)) << (L - 53)
+        vals.append(F)
+    x = np.array([np.ldexp(float(F), -83) for F in vals])
+    assert all(float(xx) * 2.0 ** 83 == float(F) for xx, F in zip(x[:1000], vals[:1000]))
+    out = gpu.probe_check(2, 8, x)
+    bad = np.nonzero(out[:, 0] != out[:, 1])[0]
+    assert len(bad) == 0, [(float.hex(float(x[i])), out[i].tolist()) for i in bad[:5]]
