@@ -273,6 +273,249 @@ def bench_spmv(torch, mp, stream, steps, warmup, world, hbm):
             "nnz": nnz}
 
 
+def device_doubles(torch, gen, count, lo, hi):
+    """u * 2^e with u ~ U(-1, 1) and e ~ U{lo..hi}, generated on the device."""
+    u = torch.rand(count, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1
+    e = torch.randint(lo, hi + 1, (count,), generator=gen, device="cuda")
+    return torch.ldexp(u, e)
+
+
+def value_pool(torch, mp, nmod, count, lo, hi, seed):
+    """count seeded u*2^e values converted on the device (bit-identical to the
+    host conversion); the large operands are filled by random draws from it."""
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    pool = mp.TensorArray(nmod, count)
+    chunk = 1 << 22
+    for off in range(0, count, chunk):
+        pool.set_d(device_doubles(torch, gen, min(chunk, count - off), lo, hi), off)
+    return pool, gen
+
+
+def fill_from_pool(torch, arr, pool, gen, offset=0, count=None):
+    count = arr.size - offset if count is None else count
+    chunk = 1 << 25
+    for off in range(0, count, chunk):
+        c = min(chunk, count - off)
+        idx = torch.randint(0, pool.size, (c,), generator=gen, device="cuda")
+        arr.gather_from(pool, idx, offset + off)
+
+
+def log_uniform_ints(rng, shape, lo, hi):
+    return np.clip(np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), shape))), lo, hi).astype(np.int64)
+
+
+def snapshot(a):
+    return [t.clone() for t in (a.digits, a.sign, a.exp, a.eval)]
+
+
+def restore(a, snap):
+    for t, v in zip((a.digits, a.sign, a.exp, a.eval), snap):
+        t.copy_(v)
+
+
+def same(a, snap):
+    import torch
+    return all(torch.equal(t, v) for t, v in zip((a.digits, a.sign, a.exp, a.eval), snap))
+
+
+def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=40 << 30):
+    """4096 mp_gemv y = alpha*A*x + beta*y (NO_TRANS, lda = m), m and n
+    log-uniform in [32, 4096], entries u*2^e with e in [-32, 32], 16 moduli:
+    one persistent launch per wave (graph replay, autotuned shape) against the
+    4096 plain mpres_gemv calls, both timed with CUDA events with operands
+    resident.  A is about 294 GB in all, so the instances run in waves of at
+    most wave_bytes of A; every A, x, y is filled with random draws from 2^23
+    seeded values converted on the device."""
+    n, rec, b3 = 16, 104, 32
+    sizes = log_uniform_ints(np.random.default_rng(SEED + 3), (count, 2), 32, 4096)
+    pool, gen = value_pool(torch, mp, n, 1 << 23, -32, 32, SEED + 3)
+    waves, cur, acc = [], [], 0
+    for i, (m, k) in enumerate(sizes):
+        b = int(m * k * rec)
+        if cur and acc + b > wave_bytes:
+            waves.append(cur)
+            cur, acc = [], 0
+        cur.append(i)
+        acc += b
+    waves.append(cur)
+    t_plain = t_batch = 0.0
+    identical, info, commit_s = True, None, 0.0
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    for w, idx in enumerate(waves):
+        M, K = sizes[idx, 0], sizes[idx, 1]
+        a_off = np.concatenate([[0], np.cumsum(M * K)])
+        x_off = np.concatenate([[0], np.cumsum(K)])
+        y_off = np.concatenate([[0], np.cumsum(M)])
+        A, X, Y = mp.TensorArray(n, int(a_off[-1])), mp.TensorArray(n, int(x_off[-1])), mp.TensorArray(n, int(y_off[-1]))
+        AB = mp.TensorArray(n, 2 * len(idx))
+        for arr in (A, X, Y):
+            fill_from_pool(torch, arr, pool, gen)
+        AB.set_d(torch.rand(2 * len(idx), generator=gen, device="cuda", dtype=torch.float64) * 2 - 1)
+        ops = [(int(M[j]), int(K[j]), AB.view(2 * j, 1), A.view(int(a_off[j]), int(M[j] * K[j])),
+                X.view(int(x_off[j]), int(K[j])), AB.view(2 * j + 1, 1), Y.view(int(y_off[j]), int(M[j])))
+               for j in range(len(idx))]
+        torch.cuda.synchronize()
+
+        def plain():
+            for m, k, al, Av, xv, be, yv in ops:
+                mp.gemv(n, mp.NO_TRANS, m, k, al, Av, m, xv, be, yv, order=(256, 128, 256, b3), stream=stream)
+
+        batch = mp.Batch(n)
+        for m, k, al, Av, xv, be, yv in ops:
+            batch.add_gemv(mp.NO_TRANS, m, k, al, Av, m, xv, be, yv, b3=b3)
+        t0 = time.perf_counter()
+        batch.commit(mp.BATCH_GRAPH | (mp.BATCH_AUTOTUNE if w == 0 else 0), stream=stream)
+        torch.cuda.synchronize()
+        commit_s += time.perf_counter() - t0
+        if w == 0:
+            info = batch.info()
+            y0 = snapshot(Y)
+            plain()
+            torch.cuda.synchronize()
+            yp = snapshot(Y)
+            restore(Y, y0)
+            batch.run(stream)
+            torch.cuda.synchronize()
+            identical = same(Y, yp)
+        batch.run(stream)  # warm (graph upload)
+        ev[0].record(stream)
+        plain()
+        ev[1].record(stream)
+        ev[2].record(stream)
+        batch.run(stream)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        t_plain += ev[0].elapsed_time(ev[1]) / 1e3
+        t_batch += ev[2].elapsed_time(ev[3]) / 1e3
+        batch.destroy()
+        del A, X, Y, AB, ops
+        torch.cuda.empty_cache()
+    mk = sizes[:, 0] * sizes[:, 1]
+    ops_total = float(np.sum(2 * mk))
+    algo = float(np.sum((mk + sizes[:, 1] + 2 * sizes[:, 0]) * rec))
+    return {"workload": "4096 x mp_gemv NO_TRANS, m, n log-uniform in [32, 4096], 16 moduli, blockDim3 = 32",
+            "value": ops_total / t_batch, "unit": "MP ops/s", "plain_value": ops_total / t_plain,
+            "speedup_vs_plain": t_plain / t_batch, "ms_batched": t_batch * 1e3, "ms_plain": t_plain * 1e3,
+            "waves": len(waves), "wave_bytes_max": wave_bytes, "launches_batched": 2 * len(waves),
+            "launches_plain": 2 * count, "bit_identical_first_wave": identical, "shape": info,
+            "commit_s": commit_s,
+            "roofline": {"bound": "hbm", "achieved": algo / t_batch / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": algo / t_batch / 1e9 / hbm, "traffic": None},
+            "data": "A, x, y: random draws from 2^23 seeded u*2^e values (e in [-32, 32]) converted on the GPU; "
+                    "alpha, beta ~ U(-1, 1)"}
+
+
+def bench_serving(torch, mp, rates=(100.0, 400.0, 1600.0), duration=1.5, budget=64 << 30):
+    """Poisson request streams mixing mp_dot (n log-uniform 2^10..2^22),
+    mp_gemv (m, n log-uniform 32..4096) and mp_spmv_csr (rows log-uniform
+    2^12..2^20, power-law rows), 8 moduli, operands resident, through the
+    serving loop (64 GB budget, 4 batches in flight).  Each request draws one
+    of a pool of resident operand sets of its kind; GEMV and DOT outputs are
+    its own.  Reports per offered rate: throughput, p50 / p99 latency."""
+    n, rec = 8, 72
+    rng = np.random.default_rng(SEED + 4)
+    pool, gen = value_pool(torch, mp, n, 1 << 22, -16, 16, SEED + 4)
+    dots = []
+    for cnt in log_uniform_ints(rng, 8, 1 << 10, 1 << 22):
+        x, y = mp.TensorArray(n, int(cnt)), mp.TensorArray(n, int(cnt))
+        fill_from_pool(torch, x, pool, gen)
+        fill_from_pool(torch, y, pool, gen)
+        dots.append((int(cnt), x, y))
+    gemvs = []
+    for m, k in log_uniform_ints(rng, (8, 2), 32, 4096):
+        A, x, y0 = mp.TensorArray(n, int(m * k)), mp.TensorArray(n, int(k)), mp.TensorArray(n, int(m))
+        for a in (A, x, y0):
+            fill_from_pool(torch, a, pool, gen)
+        ab = mp.TensorArray(n, 2)
+        ab.set_d(torch.rand(2, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1)
+        gemvs.append((int(m), int(k), A, x, y0, ab))
+    spmvs = []
+    for m in log_uniform_ints(rng, 4, 1 << 12, 1 << 20):
+        m = int(m)
+        irp, ja, vals = random_csr(rng, m, m, power_law_rows(rng, m))
+        xs = mp.TensorArray(n, m)  # x as AoS records (mp_float_t*) for the CSR kernel
+        fill_from_pool(torch, xs, pool, gen)
+        xa = mp.DeviceBytes.from_numpy(xs.download())
+        spmvs.append((m, int(irp[-1]), mp.DeviceCsr(m, irp, ja, vals), xa, mp.DeviceBytes(m * rec)))
+    torch.cuda.synchronize()
+    results = []
+    checks = []
+    for rate in rates:
+        count = max(60, int(rate * duration))
+        kinds = rng.integers(0, 3, count)
+        picks = rng.integers(0, 8, count)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+        outs_r = mp.TensorArray(n, count)
+        gy_len = [gemvs[p][0] if k == 1 else 0 for k, p in zip(kinds, picks)]
+        gy_off = np.concatenate([[0], np.cumsum(gy_len)])
+        outs_y = mp.TensorArray(n, max(1, int(gy_off[-1])))
+        for i in range(count):  # every GEMV request starts from its operand set's y
+            if kinds[i] == 1:
+                y0 = gemvs[picks[i]][4]
+                outs_y.gather_from(y0, torch.arange(y0.size, device="cuda"), int(gy_off[i]))
+        y_init = snapshot(outs_y)
+        torch.cuda.synchronize()
+        srv = mp.Server(n, budget, slots=4, max_batch_ops=64)
+        ops_total = 0.0
+        t_start = time.perf_counter()
+        for i in range(count):
+            while time.perf_counter() - t_start < arrivals[i]:
+                pass
+            k, p = int(kinds[i]), int(picks[i])
+            if k == 0:
+                cnt, x, y = dots[p]
+                srv.submit_dot(cnt, x, y, outs_r.view(i, 1))
+                ops_total += 2.0 * cnt
+            elif k == 1:
+                m, kk, A, x, _, ab = gemvs[p]
+                srv.submit_gemv(mp.NO_TRANS, m, kk, ab.view(0, 1), A, m, x, ab.view(1, 1),
+                                outs_y.view(int(gy_off[i]), m))
+                ops_total += 2.0 * m * kk
+            else:
+                m, nnz, csr, xa, ya = spmvs[p % len(spmvs)]
+                srv.submit_spmv_csr(m, m, csr, xa, ya)
+                ops_total += 2.0 * nnz
+        srv.drain()
+        st = srv.stats()
+        t = srv.times(0, count)
+        srv.destroy()
+        span = float(t[:, 2].max() - t[:, 0].min())
+        results.append({"offered_per_s": rate, "requests": count, "throughput_per_s": count / span,
+                        "mp_ops_per_s": ops_total / span, "p50_ms": st["p50_s"] * 1e3, "p99_ms": st["p99_s"] * 1e3,
+                        "mean_batch": st["mean_batch"], "max_in_flight": st["max_in_flight"],
+                        "peak_admitted_gb": st["peak_bytes"] / 1e9})
+        # a sample of requests rerun alone through the plain calls: identical records
+        sample = [i for i in range(count) if kinds[i] != 2][:12]
+        mix_y, mix_r = snapshot(outs_y), snapshot(outs_r)
+        restore(outs_y, y_init)
+        for i in sample:
+            p = int(picks[i])
+            if kinds[i] == 0:
+                cnt, x, y = dots[p]
+                mp.dot(n, cnt, x, y, outs_r.view(i, 1))
+            else:
+                m, kk, A, x, _, ab = gemvs[p]
+                mp.gemv(n, mp.NO_TRANS, m, kk, ab.view(0, 1), A, m, x, ab.view(1, 1), outs_y.view(int(gy_off[i]), m))
+        torch.cuda.synchronize()
+        for i in sample:
+            arr, snap, off, cnt = ((outs_r, mix_r, i, 1) if kinds[i] == 0 else
+                                   (outs_y, mix_y, int(gy_off[i]), gemvs[int(picks[i])][0]))
+            checks.append(all(torch.equal(a[sl], b[sl]) for a, b, sl in _record_slices(arr, snap, off, cnt)))
+        del outs_r, outs_y
+    return {"workload": "Poisson mix of mp_dot (n 2^10..2^22), mp_gemv (m, n 32..4096), mp_spmv_csr (rows 2^12..2^20), "
+                        "8 moduli, 64 GB budget, 4 batches in flight",
+            "rates": results, "alone_vs_mix_identical": bool(checks) and all(checks), "checked_requests": len(checks)}
+
+
+def _record_slices(arr, snap, off, cnt):
+    """(current tensor, snapshot tensor, slice) triples covering elements [off, off + cnt) of a TensorArray."""
+    n = arr.nmod
+    return [(arr.digits, snap[0], slice(off * n, (off + cnt) * n)), (arr.sign, snap[1], slice(off, off + cnt)),
+            (arr.exp, snap[2], slice(off, off + cnt)), (arr.eval, snap[3], slice(off, off + cnt)),
+            (arr.eval, snap[3], slice(arr.size + off, arr.size + off + cnt))]
+
+
 # ------------------------------------------------------------ CPU baseline --
 
 def cpu_gemm_sample(host, budget_s=12.0):
@@ -292,12 +535,41 @@ def cpu_gemm_sample(host, budget_s=12.0):
 
     rows, cols = 8, 2
     t = time_block(rows, cols)
-    while t < budget_s / 8 and cols < m:
-        cols = min(m, cols * 2)
+    while t < budget_s / 2 and (cols < m or rows < m):
+        if cols < m:
+            cols = min(m, cols * 2)
+        else:
+            rows = min(m, rows * 2)
         t = time_block(rows, cols)
     ops = 2.0 * rows * cols * m + 3.0 * rows * cols
     return {"value": ops / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
             "sample": "oracle mp_gemm on a %dx%d block of C (k = 1024, 32 moduli), %.1f s" % (rows, cols, t)}
+
+
+def cpu_gemv_sample(torch, mp, budget_s=6.0):
+    """The oracle port on the first instances of the batched-GEMV workload (sizes
+    as there, fresh seeded entries), until budget_s; MP ops/s."""
+    from oracle import ffi
+    O = ffi.oracle()
+    n = 16
+    sizes = log_uniform_ints(np.random.default_rng(SEED + 3), (4096, 2), 32, 4096)
+    rng = np.random.default_rng(SEED + 30)
+    ops = t = 0.0
+    done = 0
+    for m, k in sizes:
+        m, k = int(m), int(k)
+        A = mp.set_d(n, doubles(rng, m * k, -32, 32))
+        x, y = mp.set_d(n, doubles(rng, k, -32, 32)), mp.set_d(n, doubles(rng, m, -32, 32))
+        ab = mp.set_d(n, rng.uniform(-1, 1, 2))
+        t0 = time.perf_counter()
+        O.gemv(n, mp.NO_TRANS, m, k, ab[:1], A, m, x, ab[1:], y, b3=32)
+        t += time.perf_counter() - t0
+        ops += 2.0 * m * k
+        done += 1
+        if t > budget_s:
+            break
+    return {"value": ops / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
+            "sample": "oracle mp_gemv on the first %d of the 4096 instances, %.1f s" % (done, t)}
 
 
 def cpu_dot_sample(mx, my, budget_s=6.0):
@@ -323,6 +595,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extra", action="store_true", help="headline GEMM only")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-GEMV and serving workloads")
     args = ap.parse_args()
     world, rank, local = dist()
 
@@ -374,6 +647,9 @@ def main():
         spmv = bench_spmv(torch, mp, stream, 5, 2, world, hbm)
         extra["mp_dot"] = {k: v for k, v in dot.items() if k != "data"}
         extra["mp_spmv"] = spmv
+        if not args.no_batch:
+            extra["batched_gemv"] = bench_batched_gemv(torch, mp, stream, hbm)
+            extra["serving"] = bench_serving(torch, mp)
     line = {
         "metric": METRIC, "value": g["value"], "unit": "MP ops/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": g["secs"] / args.steps * 1e3, "higher_is_better": True,
@@ -390,6 +666,8 @@ def main():
         line["cpu_baseline"] = cpu_gemm_sample(g["host"])
         if not args.no_extra:
             line["mp_dot"]["cpu_baseline"] = cpu_dot_sample(*dot["data"])
+            if "batched_gemv" in line:
+                line["batched_gemv"]["cpu_baseline"] = cpu_gemv_sample(torch, mp)
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as td

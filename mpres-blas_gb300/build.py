@@ -20,7 +20,7 @@ INCLUDE = HERE.parent / "include"
 
 CU_SOURCES = ["dot.cu", "gemv.cu", "gemm.cu", "spmv.cu", "capi.cu", "probe.cu", "elementwise.cu", "convert.cu",
               "batch.cu"]
-CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp"]
+CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp", "server.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -72,7 +72,7 @@ def build(verbose=False, ptxas_info=False):
         src, obj = CSRC / s, OUT / (s + ".o")
         objs.append(obj)
         if _stale(obj, src):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math",
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math",
                          "-I", str(CSRC), "-I", str(home / "include"), "-c", str(src), "-o", str(obj)])
     logs = []
     if jobs:

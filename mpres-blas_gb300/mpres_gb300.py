@@ -75,6 +75,15 @@ _SIGS = {
     "mpres_batch_commit": (I, [P, ctypes.c_uint, P]),
     "mpres_batch_run": (I, [P, P]),
     "mpres_batch_info": (I, [P, P]),
+    "mpres_server_create": (I, [I, SZ, I, I, P]),
+    "mpres_server_destroy": (I, [P]),
+    "mpres_server_submit_gemv": (I, [P, I, I, I, P, P, I, P, I, P, P, I, I, P]),
+    "mpres_server_submit_dot": (I, [P, I, P, I, P, I, P, I, I, P]),
+    "mpres_server_submit_spmv_csr": (I, [P, I, I, ctypes.c_longlong, P, P, P, P]),
+    "mpres_server_wait": (I, [P, ctypes.c_longlong, ctypes.c_double]),
+    "mpres_server_drain": (I, [P]),
+    "mpres_server_times": (I, [P, ctypes.c_longlong, ctypes.c_longlong, P]),
+    "mpres_server_stats": (I, [P, P]),
     "mpres_probe_mulmod": (I, [I, I, ctypes.c_longlong, P, P]),
     "mpres_probe_dadd": (I, [I, I, ctypes.c_longlong, P, P]),
     "mpres_elementwise": (I, [I, I, P, P, P, SZ, P]),
@@ -199,6 +208,73 @@ class DeviceArray:
                 self._live = False
         except Exception:
             pass
+
+
+class TensorArray:
+    """An mp_array_t whose SoA fields are torch CUDA tensors (digits int32
+    [size*nmod], sign and exp int32 [size], eval int64 [2*size, 2] holding the
+    er_float_t {frac, exp} pairs of the lower then the upper bounds).  view()
+    gives mp_array_t views of contiguous element ranges: their fields point
+    into this array and share its len, so a view's upper bounds are found where
+    the kernels look for them (eval + len)."""
+
+    def __init__(self, nmod, size, device="cuda"):
+        import torch
+        self.nmod, self.size = nmod, int(size)
+        self.digits = torch.empty(self.size * nmod, dtype=torch.int32, device=device)
+        self.sign = torch.empty(self.size, dtype=torch.int32, device=device)
+        self.exp = torch.empty(self.size, dtype=torch.int32, device=device)
+        self.eval = torch.empty((2 * self.size, 2), dtype=torch.int64, device=device)
+        self.len = torch.tensor([self.size], dtype=torch.int32, device=device)
+        self.a = self._struct(0)
+
+    def _struct(self, off):
+        return MpArrayT(self.digits.data_ptr() + 4 * self.nmod * off, self.sign.data_ptr() + 4 * off,
+                        self.exp.data_ptr() + 4 * off, self.eval.data_ptr() + 16 * off, None, self.len.data_ptr())
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.a)
+
+    def view(self, offset, length):
+        if offset < 0 or offset + length > self.size:
+            raise MpresError("TensorArray.view: [%d, %d) outside %d elements" % (offset, offset + length, self.size))
+        return _ArrayView(self, self._struct(offset), length)
+
+    def gather_from(self, src, index, offset=0):
+        """Elements [offset, offset + len(index)) = src[index] (src a TensorArray)."""
+        k = index.numel()
+        n = self.nmod
+        self.digits.view(-1, n)[offset:offset + k] = src.digits.view(-1, n).index_select(0, index)
+        self.sign[offset:offset + k] = src.sign.index_select(0, index)
+        self.exp[offset:offset + k] = src.exp.index_select(0, index)
+        self.eval[offset:offset + k] = src.eval[: src.size].index_select(0, index)
+        self.eval[self.size + offset:self.size + offset + k] = src.eval[src.size:].index_select(0, index)
+
+    def set_d(self, x, offset=0, stream=None):
+        """Device conversion of a float64 CUDA tensor into elements [offset, offset + x.numel())."""
+        array_set_d(self.nmod, self, offset, x, stream)
+
+    def download(self):
+        out = np.zeros(self.size, mp_dtype(self.nmod))
+        out["digits"] = self.digits.view(-1, self.nmod).cpu().numpy()
+        out["sign"] = self.sign.cpu().numpy()
+        out["exp"] = self.exp.cpu().numpy()
+        ev = self.eval.cpu().numpy()
+        for h in (0, 1):
+            half = ev[h * self.size:(h + 1) * self.size]
+            out["eval"][:, h]["frac"] = half[:, 0].view(np.float64)
+            out["eval"][:, h]["exp"] = half[:, 1]
+        return out
+
+
+class _ArrayView:
+    def __init__(self, owner, struct, size):
+        self.owner, self.a, self.size, self.nmod = owner, struct, size, owner.nmod
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.a)
 
 
 class DeviceBytes:
@@ -345,6 +421,69 @@ class Batch:
         if self.h:
             check(lib().mpres_batch_destroy(self.h), "mpres_batch_destroy")
             self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Server:
+    """The serving loop (include/mpres_gb300_server.h): requests over
+    device-resident operands, admitted under an HBM budget and run as
+    continuous batches.  Operands must stay alive until their request is done."""
+
+    def __init__(self, nmod, budget_bytes, slots=4, max_batch_ops=64):
+        self.nmod = nmod
+        self.h = ctypes.c_void_p()
+        check(lib().mpres_server_create(nmod, int(budget_bytes), slots, max_batch_ops, ctypes.byref(self.h)),
+              "mpres_server_create")
+        self._keep = {}
+
+    def submit_gemv(self, trans, m, n, alpha, A, lda, x, beta, y, incx=1, incy=1, b3=32):
+        i = ctypes.c_longlong()
+        check(lib().mpres_server_submit_gemv(self.h, trans, m, n, alpha.ref, A.ref, lda, x.ref, incx, beta.ref,
+                                             y.ref, incy, b3, ctypes.byref(i)), "mpres_server_submit_gemv")
+        self._keep[i.value] = (alpha, A, x, beta, y)
+        return i.value
+
+    def submit_dot(self, n, x, y, r, incx=1, incy=1, g3=256, b3=64):
+        i = ctypes.c_longlong()
+        check(lib().mpres_server_submit_dot(self.h, n, x.ref, incx, y.ref, incy, r.ref, g3, b3, ctypes.byref(i)),
+              "mpres_server_submit_dot")
+        self._keep[i.value] = (x, y, r)
+        return i.value
+
+    def submit_spmv_csr(self, m, ncols, csr, x, y):
+        i = ctypes.c_longlong()
+        check(lib().mpres_server_submit_spmv_csr(self.h, m, ncols, csr.nnz, ctypes.byref(csr.c), x.ptr, y.ptr,
+                                                 ctypes.byref(i)), "mpres_server_submit_spmv_csr")
+        self._keep[i.value] = (csr, x, y)
+        return i.value
+
+    def wait(self, rid, timeout=-1.0):
+        check(lib().mpres_server_wait(self.h, rid, timeout), "mpres_server_wait")
+
+    def drain(self):
+        check(lib().mpres_server_drain(self.h), "mpres_server_drain")
+
+    def times(self, first, count):
+        out = np.zeros(3 * count)
+        check(lib().mpres_server_times(self.h, first, count, out.ctypes.data), "mpres_server_times")
+        return out.reshape(count, 3)
+
+    def stats(self):
+        out = np.zeros(8)
+        check(lib().mpres_server_stats(self.h, out.ctypes.data), "mpres_server_stats")
+        keys = ("done", "batches", "mean_batch", "p50_s", "p99_s", "peak_bytes", "max_in_flight", "errors")
+        return dict(zip(keys, out.tolist()))
+
+    def destroy(self):
+        if self.h:
+            h, self.h = self.h, ctypes.c_void_p()
+            check(lib().mpres_server_destroy(h), "mpres_server_destroy")
+            self._keep.clear()
 
     def __del__(self):
         try:
