@@ -118,6 +118,23 @@ int mpres_ell_init(ell_t *ell, int m, int maxnzr);
 int mpres_ell_host2device(ell_t *dev, const ell_t *host, int m, int maxnzr);
 int mpres_ell_clear(ell_t *ell);
 
+/* ---- Matrix Market files (host) ----------------------------------------- */
+
+/* collect_mtx_stats (src/sparse/utils/mtx_reader.cuh:52-101): sizes of a
+ * coordinate file, the longest row (mirrored entries of a symmetric matrix
+ * counted), the diagonal entries, symmetry, and the data type ("real" or
+ * "integer"; datatype may be NULL, else 16 bytes).  Pattern and complex files
+ * are rejected with MPRES_ERR_NOT_SUPPORTED. */
+int mpres_mtx_stats(const char *path, int *m, int *n, int *lines, int *maxnzr, int *nzmd, int *symmetric,
+                    char *datatype);
+/* build_csr (mtx_reader.cuh:200-253): as[nnz], ja[nnz], irp[m + 1], host arrays
+ * the caller allocates; nnz = lines, or 2*(lines - nzmd) + nzmd if symmetric.
+ * The entry order within rows is the reference's, so SpMV results match. */
+int mpres_mtx_build_csr(const char *path, int m, int nnz, int lines, int symmetric, double *as, int *ja, int *irp);
+/* build_ell (mtx_reader.cuh:374-406): as[m*maxnzr], ja[m*maxnzr], column-major,
+ * padding 0.0 / -1. */
+int mpres_mtx_build_ell(const char *path, int m, int maxnzr, int lines, int symmetric, double *as, int *ja);
+
 /* ---- conversion --------------------------------------------------------- */
 
 /* mp_set_d (src/arith/assign.cuh:54-81), host: x[count] -> mp_float_t[count]. */
@@ -134,6 +151,22 @@ int mpres_set_d(int nmod, const double *x, size_t count, void *out);
  * host behaviour, which no finite double is known to do). */
 int mpres_set_d_device(int nmod, const double *x, size_t count, void *out, void *stream);
 int mpres_array_set_d(int nmod, mp_array_t *dst, size_t offset, const double *x, size_t count, void *stream);
+
+/* ---- host MPFR operations ------------------------------------------------ */
+
+/* ::mp_div (src/arith/div.cuh:33-45), ::mp_sqrt and ::mp_dsqrt (src/arith/sqrt.cuh):
+ * the operands rounded to MP_PRECISION bits, the correctly rounded (nearest-even)
+ * quotient or root at MP_PRECISION bits, converted back as mp_set_mpfr does
+ * (mp_dsqrt: rounded again to a double).  Host mp_float_t records; exact
+ * integer arithmetic gives MPFR's bits without MPFR.  Division by zero and
+ * roots of negative numbers return MPRES_ERR_INVALID_VALUE. */
+int mpres_div(int nmod, const void *x, const void *y, void *r);
+int mpres_sqrt(int nmod, const void *x, void *r);
+int mpres_dsqrt(int nmod, const void *x, double *out);
+/* cuda::mp_div and cuda::mp_dsqrt (src/arith/div.cuh:56-65, sqrt.cuh): the same
+ * with the records in device memory (synchronous copies, host computation). */
+int mpres_div_device(int nmod, const void *x, const void *y, void *r);
+int mpres_dsqrt_device(int nmod, const void *x, double *out);
 
 /* ---- BLAS ---------------------------------------------------------------- */
 

@@ -28,6 +28,7 @@
 #define MPRES_GB300_HPP
 
 #include <cstdio>
+#include <string>
 
 #include "mpres_gb300.h"
 
@@ -132,5 +133,24 @@ template <int threads> void mp_spmv_ell(const int m, const int maxnzr, const ell
 }
 
 } // namespace cuda
+
+/* src/sparse/utils/mtx_reader.cuh:52, :249, :374 (global functions in the reference) */
+inline void collect_mtx_stats(const char *filename, int &m, int &n, int &lines, int &maxnzr, int &nzmd,
+                              bool &symmetric, std::string &datatype) {
+    int sym = 0;
+    char dt[16] = {0};
+    mpres_detail::report(mpres_mtx_stats(filename, &m, &n, &lines, &maxnzr, &nzmd, &sym, dt), "collect_mtx_stats");
+    symmetric = sym != 0;
+    datatype = dt;
+}
+inline void build_csr(const char filename[], const int m, const int nnz, const int lines, const bool symmetric,
+                      csr_t &csr) {
+    mpres_detail::report(mpres_mtx_build_csr(filename, m, nnz, lines, symmetric, csr.as, csr.ja, csr.irp),
+                         "build_csr");
+}
+inline void build_ell(const char filename[], const int m, const int maxnzr, const int lines, const bool symmetric,
+                      ell_t &ell) {
+    mpres_detail::report(mpres_mtx_build_ell(filename, m, maxnzr, lines, symmetric, ell.as, ell.ja), "build_ell");
+}
 
 #endif

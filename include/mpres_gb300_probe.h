@@ -19,6 +19,10 @@ extern "C" {
 
 int mpres_probe_mulmod(int blocks, int threads, long long iters, void *sink, void *stream);
 int mpres_probe_dadd(int blocks, int threads, long long iters, void *sink, void *stream);
+/* Latency of one dependent operation in SM cycles, measured by one thread over
+ * `iters` operations: which 0 = __dadd_rd, 1 = Barrett modular product,
+ * 2 = 64-bit shift-add; out = device double[2], out[0] receives the cycles. */
+int mpres_probe_latency(int which, long long iters, void *out, void *stream);
 
 /* out[i] = ceil(log2(x[i])) with the CUDA math library, the expression the
  * reference's interval-evaluation refinement loop evaluates on the device
@@ -32,7 +36,9 @@ int mpres_probe_ceil_log2(const double *x, double *out, size_t count, void *stre
  *   which 1: exponent-field scaling, a = double[count], b = int[count],
  *            out = double[2*count]: {scale2(a, b), scalbn(a, b)};
  *   which 2: ceil(log2) of fixed-point fractions, a = double[count] (multiples of
- *            2^-83 below 1), out = int[2*count]: {from bits, ceil(log2(a))}.
+ *            2^-83 below 1), out = int[2*count]: {from bits, ceil(log2(a))};
+ *   which 3: ceil(log2) of any positive doubles, a = double[count],
+ *            out = int[2*count]: {from bits, ceil(log2(a))}.
  * All pointers are device memory. */
 int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *out, size_t count, void *stream);
 

@@ -20,7 +20,7 @@ INCLUDE = HERE.parent / "include"
 
 CU_SOURCES = ["dot.cu", "gemv.cu", "gemm.cu", "spmv.cu", "capi.cu", "probe.cu", "elementwise.cu", "convert.cu",
               "batch.cu"]
-CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp", "server.cpp"]
+CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp", "host_mpfr.cpp", "server.cpp", "mtx.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -5,6 +5,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -20,6 +21,9 @@
 
 namespace mpres {
 void host_set_d(const HostTables &t, const double *x, size_t count, void *out);
+bool host_mp_div(const HostTables &t, const void *x, const void *y, void *r);
+bool host_mp_sqrt(const HostTables &t, const void *x, void *r);
+bool host_mp_dsqrt(const HostTables &t, const void *x, double &out);
 }
 
 using namespace mpres;
@@ -66,6 +70,8 @@ struct WsKey {
     bool operator<(const WsKey &o) const { return device != o.device ? device < o.device : stream < o.stream; }
 };
 std::map<WsKey, Workspace> g_ws;
+Workspace g_staging[64]; /* per device: records in transit for the array copies */
+std::mutex g_copy_mu;
 
 /* ceil(log2(2^e)) for e = -1074..1023 with CUDA's log2, the values the
  * reference's refinement loop takes at exact powers of two (fixed_eval.cuh) */
@@ -289,54 +295,56 @@ int mpres_array_clear(mp_array_t *a) {
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_array_clear");
 }
 
+/* Bulk copies between host mp_float_t records and a device mp_array_t: the
+ * records travel as they are, in chunks through a device staging buffer, and a
+ * kernel packs them into (or out of) the SoA fields.  The reference issues one
+ * cudaMemcpy per element for the digits and packs sign, exp and eval on the
+ * host (src/mparray.cuh:76-160); like it, the copies are synchronous, and the
+ * upper bounds are placed `size` elements after the lower ones. */
+static int array_copy(const char *what, int nmod, bool to_device, mp_array_t *a, char *host, size_t size) {
+    const size_t rec = mp_size(nmod);
+    const size_t chunk = std::max<size_t>(1, std::min<size_t>(size, ((size_t)256 << 20) / rec));
+    cudaError_t e;
+    std::lock_guard<std::mutex> lk(g_copy_mu); /* one copy at a time uses the staging buffer */
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_fail(e, what);
+    Workspace &w = g_staging[dev < 64 ? dev : 0];
+    if (w.bytes < chunk * rec) {
+        if (w.ptr) cudaFree(w.ptr);
+        w.ptr = nullptr;
+        w.bytes = 0;
+        if ((e = cudaMalloc(&w.ptr, chunk * rec)) != cudaSuccess) return cuda_fail(e, what);
+        w.bytes = chunk * rec;
+    }
+    void *staging = w.ptr;
+    for (size_t off = 0; off < size; off += chunk) {
+        const size_t c = std::min(chunk, size - off);
+        if (to_device) {
+            if ((e = cudaMemcpy(staging, host + off * rec, c * rec, cudaMemcpyHostToDevice)) != cudaSuccess ||
+                (e = launch_pack(nmod, true, staging, *a, (long long)size, (long long)off, (long long)c, 0)) != cudaSuccess)
+                return cuda_fail(e, what);
+        } else {
+            if ((e = launch_pack(nmod, false, staging, *a, (long long)size, (long long)off, (long long)c, 0)) != cudaSuccess ||
+                (e = cudaMemcpy(host + off * rec, staging, c * rec, cudaMemcpyDeviceToHost)) != cudaSuccess)
+                return cuda_fail(e, what);
+        }
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return cuda_fail(e, what);
+    return ok();
+}
+
 int mpres_array_host2device(int nmod, mp_array_t *dst, const void *host_src, size_t size) {
     if (!dst || (!host_src && size) || set_slot(nmod) < 0)
         return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_host2device: bad arguments");
     if (size == 0) return ok();
-    const size_t sz = mp_size(nmod);
-    std::vector<int> digits((size_t)nmod * size), sign(size), exp(size);
-    std::vector<er_float_t> eval(2 * size);
-    const char *src = static_cast<const char *>(host_src);
-    for (size_t i = 0; i < size; i++) {
-        const char *p = src + i * sz;
-        std::memcpy(&digits[i * nmod], p, 4 * (size_t)nmod);
-        std::memcpy(&sign[i], p + 4 * nmod, 4);
-        std::memcpy(&exp[i], p + 4 * nmod + 4, 4);
-        std::memcpy(&eval[i], p + 4 * nmod + 8, 16);
-        std::memcpy(&eval[size + i], p + 4 * nmod + 24, 16);
-    }
-    cudaError_t e;
-    if ((e = cudaMemcpy(dst->digits, digits.data(), 4 * digits.size(), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(dst->sign, sign.data(), 4 * size, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(dst->exp, exp.data(), 4 * size, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(dst->eval, eval.data(), sizeof(er_float_t) * 2 * size, cudaMemcpyHostToDevice)) != cudaSuccess)
-        return cuda_fail(e, "mpres_array_host2device");
-    return ok();
+    return array_copy("mpres_array_host2device", nmod, true, dst, (char *)host_src, size);
 }
 
 int mpres_array_device2host(int nmod, void *host_dst, const mp_array_t *src, size_t size) {
     if (!src || (!host_dst && size) || set_slot(nmod) < 0)
         return fail(MPRES_ERR_INVALID_VALUE, "mpres_array_device2host: bad arguments");
     if (size == 0) return ok();
-    const size_t sz = mp_size(nmod);
-    std::vector<int> digits((size_t)nmod * size), sign(size), exp(size);
-    std::vector<er_float_t> eval(2 * size);
-    cudaError_t e;
-    if ((e = cudaMemcpy(digits.data(), src->digits, 4 * digits.size(), cudaMemcpyDeviceToHost)) != cudaSuccess ||
-        (e = cudaMemcpy(sign.data(), src->sign, 4 * size, cudaMemcpyDeviceToHost)) != cudaSuccess ||
-        (e = cudaMemcpy(exp.data(), src->exp, 4 * size, cudaMemcpyDeviceToHost)) != cudaSuccess ||
-        (e = cudaMemcpy(eval.data(), src->eval, sizeof(er_float_t) * 2 * size, cudaMemcpyDeviceToHost)) != cudaSuccess)
-        return cuda_fail(e, "mpres_array_device2host");
-    char *dst = static_cast<char *>(host_dst);
-    for (size_t i = 0; i < size; i++) {
-        char *p = dst + i * sz;
-        std::memcpy(p, &digits[i * nmod], 4 * (size_t)nmod);
-        std::memcpy(p + 4 * nmod, &sign[i], 4);
-        std::memcpy(p + 4 * nmod + 4, &exp[i], 4);
-        std::memcpy(p + 4 * nmod + 8, &eval[i], 16);
-        std::memcpy(p + 4 * nmod + 24, &eval[size + i], 16);
-    }
-    return ok();
+    return array_copy("mpres_array_device2host", nmod, false, const_cast<mp_array_t *>(src), (char *)host_dst, size);
 }
 
 int mpres_csr_init(csr_t *csr, int m, int nnz) {
@@ -397,6 +405,71 @@ int mpres_ell_clear(ell_t *ell) {
     std::memset(ell, 0, sizeof(*ell));
     cudaError_t e = cudaDeviceSynchronize();
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_ell_clear");
+}
+
+/* the host tables of a set, computed on first use */
+static int host_tables_of(int nmod, const char *what, const HostTables *&t) {
+    const int slot = set_slot(nmod);
+    if (slot < 0) return fail(MPRES_ERR_INVALID_VALUE, "%s: unsupported moduli set size %d", what, nmod);
+    std::lock_guard<std::mutex> lk(g_mu);
+    SetState &st = g_sets[slot];
+    if (!st.host_ready) {
+        if (!compute_host_tables(nmod, st.host)) return fail(MPRES_ERR_INVALID_VALUE, "tables of set %d", nmod);
+        st.host_ready = true;
+    }
+    t = &st.host;
+    return MPRES_SUCCESS;
+}
+
+int mpres_div(int nmod, const void *x, const void *y, void *r) {
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_div", t)) return st;
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_div: null argument");
+    if (!host_mp_div(*t, x, y, r)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_div: division by zero");
+    return ok();
+}
+
+int mpres_sqrt(int nmod, const void *x, void *r) {
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_sqrt", t)) return st;
+    if (!x || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_sqrt: null argument");
+    if (!host_mp_sqrt(*t, x, r)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_sqrt: negative operand");
+    return ok();
+}
+
+int mpres_dsqrt(int nmod, const void *x, double *out) {
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_dsqrt", t)) return st;
+    if (!x || !out) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dsqrt: null argument");
+    if (!host_mp_dsqrt(*t, x, *out)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dsqrt: negative operand");
+    return ok();
+}
+
+/* the cuda:: forms: operands and result in device memory, computed on the host */
+int mpres_div_device(int nmod, const void *x, const void *y, void *r) {
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_div_device", t)) return st;
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_div_device: null argument");
+    const size_t sz = mp_size(nmod);
+    char a[168], b[168], q[168];
+    cudaError_t e;
+    if ((e = cudaMemcpy(a, x, sz, cudaMemcpyDeviceToHost)) != cudaSuccess ||
+        (e = cudaMemcpy(b, y, sz, cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "mpres_div_device");
+    if (!host_mp_div(*t, a, b, q)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_div_device: division by zero");
+    if ((e = cudaMemcpy(r, q, sz, cudaMemcpyHostToDevice)) != cudaSuccess) return cuda_fail(e, "mpres_div_device");
+    return ok();
+}
+
+int mpres_dsqrt_device(int nmod, const void *x, double *out) {
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_dsqrt_device", t)) return st;
+    if (!x || !out) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dsqrt_device: null argument");
+    char a[168];
+    cudaError_t e = cudaMemcpy(a, x, mp_size(nmod), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "mpres_dsqrt_device");
+    if (!host_mp_dsqrt(*t, a, *out)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dsqrt_device: negative operand");
+    return ok();
 }
 
 int mpres_set_d(int nmod, const double *x, size_t count, void *out) {

@@ -206,12 +206,52 @@ __global__ void __launch_bounds__(256) set_d_soa(const double *x, long long coun
     if (bad) atomicOr(flag, 1);
 }
 
+/* AoS mp_float_t records <-> SoA mp_array_t elements [offset, offset + count);
+ * the SoA's upper bounds sit at eval + layout_len */
+template <int N>
+__global__ void __launch_bounds__(256) aos_to_soa(const void *aos, int *digits, int *sign, int *exp, er_t *eval,
+                                                  long long layout_len, long long offset, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        mp_t<N> v;
+        load_aos<N>(v, aos, i);
+        store_soa<N>(v, digits, sign, exp, eval, (int)layout_len, offset + i);
+    }
+}
+template <int N>
+__global__ void __launch_bounds__(256) soa_to_aos(const int *digits, const int *sign, const int *exp, const er_t *eval,
+                                                  long long layout_len, long long offset, long long count, void *aos) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        mp_t<N> v;
+        load_soa<N>(v, digits, sign, exp, eval, (int)layout_len, offset + i);
+        store_aos<N>(v, aos, i);
+    }
+}
+
 int blocks_for(long long count) {
     long long b = (count + 255) / 256;
     return (int)(b < 1 ? 1 : (b > 152 * 64 ? 152 * 64 : b));
 }
 
 } // namespace
+
+cudaError_t launch_pack(int nmod, bool to_soa, void *aos, const mp_array_t &a, long long layout_len, long long offset,
+                        long long count, cudaStream_t s) {
+    const int g = blocks_for(count);
+    er_t *ev = reinterpret_cast<er_t *>(a.eval);
+#define MPRES_PACK(NN)                                                                                      \
+    if (to_soa) aos_to_soa<NN><<<g, 256, 0, s>>>(aos, a.digits, a.sign, a.exp, ev, layout_len, offset, count); \
+    else soa_to_aos<NN><<<g, 256, 0, s>>>(a.digits, a.sign, a.exp, ev, layout_len, offset, count, aos);
+    switch (nmod) {
+    case 8: MPRES_PACK(8) break;
+    case 16: MPRES_PACK(16) break;
+    case 32: MPRES_PACK(32) break;
+    default: return cudaErrorInvalidValue;
+    }
+#undef MPRES_PACK
+    return cudaGetLastError();
+}
 
 cudaError_t launch_set_d(int nmod, const double *x, long long count, void *out_aos, const mp_array_t *out_soa,
                          long long offset, int *flag, cudaStream_t s) {

@@ -136,6 +136,14 @@ __global__ void check_ceil_log2_kernel(const double *x, int *out, long long coun
     }
 }
 
+template <int N> __global__ void check_ceil_log2_double_kernel(const double *x, int *out, long long count) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+         i += (long long)gridDim.x * blockDim.x) {
+        out[2 * i] = ceil_log2_d<N>(x[i]);
+        out[2 * i + 1] = (int)ceil(log2(x[i]));
+    }
+}
+
 int blocks_for(long long count) {
     long long b = (count + 255) / 256;
     return (int)(b < 1 ? 1 : (b > 65535 ? 65535 : b));
@@ -191,6 +199,8 @@ cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void
         check_scale2_kernel<<<g, 256, 0, s>>>((const double *)a, (const int *)b, (double *)out, count);
     } else if (which == 2) {
         check_ceil_log2_kernel<8><<<g, 256, 0, s>>>((const double *)a, (int *)out, count);
+    } else if (which == 3) {
+        check_ceil_log2_double_kernel<8><<<g, 256, 0, s>>>((const double *)a, (int *)out, count);
     } else {
         return cudaErrorInvalidValue;
     }

@@ -130,32 +130,9 @@ template <int N> __device__ __forceinline__ bool fx_ge_acc(const fx &a) {
     return a.hi > hi || (a.hi == hi && a.lo >= lo);
 }
 
-/* ceil(log2(x)) exactly as CUDA's log2 gives it, x = F * 2^-83 > 0.
- * The exact ceiling follows from the bits; CUDA's log2 is within one ulp of the
- * exact logarithm, which can only move the ceiling for x within a few ulps of a
- * power of two.  At an exact power of two the answer comes from a table filled at
- * mpres_init by evaluating ceil(log2(2^e)) with CUDA's log2 on the device; for
- * any other x within 4096 ulps of a power of two, CUDA's log2 is called; beyond
- * that (where a one-ulp error cannot cross an integer: the logarithm is at least
- * 4096 ulps of x away from one, i.e. well over two ulps of the result for every
- * exponent down to -1074) the exact ceiling is the answer. */
-template <int N> __device__ __forceinline__ int fx_ceil_log2(const fx &a) {
-    const int L = fx_bitlen(a);
-    const int e = L - 1 - kFixShift; /* 2^e <= x < 2^(e+1) */
-    /* distance to 2^e and to 2^(e+1) in units of the last place of x */
-    uint64_t top, above, below;
-    if (L > 53) {
-        const int sh = L - 53;
-        top = (L > 64) ? ((a.lo >> sh) | (a.hi << (64 - sh))) : (a.lo >> sh);
-    } else {
-        top = a.lo << (53 - L);
-    }
-    above = top - (1ull << 52);   /* ulps above 2^e */
-    below = (1ull << 53) - top;   /* ulps below 2^(e+1) */
-    if (above == 0) return T<N>().ceil_log2_pow2[e + 1074];
-    if (above < 4096 || below <= 4096) return (int)ceil(log2(fx_to_double(a)));
-    return e + 1;
-}
+/* ceil(log2(x)) as CUDA's log2 gives it, x = F * 2^-83 > 0 (ceil_log2_d on the
+ * exact double) */
+template <int N> __device__ __forceinline__ int fx_ceil_log2(const fx &a) { return ceil_log2_d<N>(fx_to_double(a)); }
 
 } // namespace dev
 } // namespace mpres

@@ -163,6 +163,8 @@ void set_d(const HostTables &t, double x, char *out) {
 
 } // namespace
 
+void host_eval_digits(const HostTables &t, const int *x, er_t &low, er_t &upp) { host_eval(t, x, low, upp); }
+
 /* How ceil(std::log2(x)) -- the call of the refinement loop above -- behaves just
  * above each power of two 2^e, e = -1022..0.  out[2(e+1022)] = ceil(log2(2^e));
  * out[2(e+1022)+1] = the smallest j >= 1 with ceil(log2(2^e (1 + j 2^-52))) =

@@ -56,6 +56,11 @@ cudaError_t launch_spmv_ell(int nmod, int m, int maxnzr, const ell_t &ell, const
 cudaError_t launch_set_d(int nmod, const double *x, long long count, void *out_aos, const mp_array_t *out_soa,
                          long long offset, int *flag, cudaStream_t s);
 
+/* AoS records in device memory <-> elements [offset, offset + count) of an
+ * mp_array_t whose upper bounds start at eval + layout_len */
+cudaError_t launch_pack(int nmod, bool to_soa, void *aos, const mp_array_t &a, long long layout_len, long long offset,
+                        long long count, cudaStream_t s);
+
 cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, void *r, long long count,
                                cudaStream_t s);
 cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,

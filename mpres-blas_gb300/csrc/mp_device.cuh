@@ -231,6 +231,24 @@ template <int N, bool UP, class F> __device__ __forceinline__ double psum(const 
     return psum_node<psum_span(N), N, UP>(leaf, 0);
 }
 
+/* ceil(log2(x)) exactly as CUDA's log2 gives it, for x > 0.  The exact ceiling
+ * follows from the bits; CUDA's log2 is within one ulp of the exact logarithm,
+ * which can only move the ceiling for x within a few ulps of a power of two.  At
+ * an exact power of two the answer comes from a table filled at mpres_init by
+ * evaluating ceil(log2(2^e)) with CUDA's log2 on the device; for any other x
+ * within 4096 ulps of a power of two (and for subnormal x) CUDA's log2 is
+ * called; beyond that the logarithm is at least 4096 ulps of x away from an
+ * integer -- well over two ulps of the result for every exponent -- and the
+ * exact ceiling is the answer. */
+template <int N> __device__ __forceinline__ int ceil_log2_d(double x) {
+    const uint64_t u = dbits(x);
+    const int E = (int)((u >> 52) & 2047);
+    const uint64_t j = u & ((1ull << 52) - 1);
+    if (E != 0 && j == 0) return T<N>().ceil_log2_pow2[E - 1023 + 1074];
+    if (E == 0 || j < 4096 || j >= (1ull << 52) - 4096) return (int)ceil(log2(x));
+    return E - 1023 + 1;
+}
+
 } // namespace dev
 } // namespace mpres
 
@@ -310,9 +328,14 @@ __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &u
     const Tables<N> &t = T<N>();
     int K = 0;
     for (int guard = 0; sumu < t.eval_acc && guard < 4096; guard++) {
-        double a = -(ceil(log2(sumu)) + 1);
-        int k = (int)(a > t.ref_factor ? a : (double)t.ref_factor);
-        k = pow2_row_index<N>(k < 0 ? 0 : k);
+        int k;
+        if (!dnz(sumu)) {
+            k = t.log2m; /* log2(0): the reference's index saturates past the table */
+        } else {
+            const int c = ceil_log2_d<N>(sumu);
+            k = -(c + 1) > t.ref_factor ? -(c + 1) : t.ref_factor;
+            k = pow2_row_index<N>(k < 0 ? 0 : k);
+        }
         const int *row = t.pow2 + (size_t)k * N;
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
@@ -474,10 +497,17 @@ template <int N> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
     scale2pow<N>(r.d, (unsigned int)bits);
     eval_fast<N>(r.ev[0], r.ev[1], r.d);
 }
+/* The out-of-line calls of the rare paths take their operands through a copy:
+ * a variable whose address reaches a call lives in local memory, so passing
+ * the caller's own number would keep every number of the hot loop there. */
 template <int N> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
     if (dnz(r.ev[1].frac) && r.ev[1].exp >= T<N>().mp_h) {
         int bits = (int)(r.ev[1].exp - T<N>().mp_h + 1);
-        if (bits > 0) round_slow<N>(r, bits);
+        if (bits > 0) {
+            mp_t<N> tmp = r;
+            round_slow<N>(tmp, bits);
+            r = tmp;
+        }
     }
 }
 
@@ -536,10 +566,22 @@ template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N
     ev[1] = er_add<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
     int sign = dneg(ev[0].frac);
     if (sign != (int)dneg(ev[1].frac)) {
-        sign = sign_estimate<N>(x.d, y.d, sx, sy, gamma, theta, nzx, nzy);
+        int dx[N], dy[N]; /* copies: see round_if_needed */
+#pragma unroll
+        for (int i = 0; i < N; i++) {
+            dx[i] = x.d[i];
+            dy[i] = y.d[i];
+        }
+        sign = sign_estimate<N>(dx, dy, sx, sy, gamma, theta, nzx, nzy);
         er_t u = t.unit_low;
-        if (sign) u.frac = -u.frac;
-        ev[sign] = u;
+        /* ev[sign] = +-unit_low, without indexing ev by a runtime value (which
+         * would place ev in local memory) */
+        if (sign) {
+            u.frac = -u.frac;
+            ev[1] = u;
+        } else {
+            ev[0] = u;
+        }
     }
     r.sign = sign;
     r.exp = (ex == 0) ? ey : ex;

@@ -57,6 +57,22 @@ __global__ void probe_dadd_kernel(long long iters, double step, double *sink) {
     if (s == -1.0) sink[0] = s;
 }
 
+/* latency of one dependent operation, in SM clock cycles (one thread) */
+__global__ void probe_latency_kernel(int which, long long iters, uint32_t m, uint32_t mu, double *out) {
+    const long long t0 = clock64();
+    double d = 1.0 + threadIdx.x;
+    uint32_t a = 12345u + threadIdx.x;
+    uint64_t u = 0x9e3779b97f4a7c15ull + threadIdx.x;
+    for (long long i = 0; i < iters; i++) {
+        if (which == 0) d = __dadd_rd(d, 1e-3);
+        else if (which == 1) a = mulmod(a, 48271u, m, mu);
+        else u = (u << 3) + (u >> 7) + 1;
+    }
+    const long long t1 = clock64();
+    out[0] = (double)(t1 - t0) / (double)iters;
+    if (d == -1.0 || a == 0xffffffffu || u == 0) out[1] = d + a + (double)u; /* keeps the chains live */
+}
+
 __global__ void probe_ceil_log2_kernel(const double *x, double *out, long long count) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
          i += (long long)gridDim.x * blockDim.x)
@@ -73,6 +89,13 @@ int mpres_probe_ceil_log2(const double *x, double *out, size_t count, void *stre
     long long blocks = ((long long)count + 255) / 256;
     probe_ceil_log2_kernel<<<(int)(blocks > 65535 ? 65535 : blocks), 256, 0, (cudaStream_t)stream>>>(
         x, out, (long long)count);
+    return cudaGetLastError() == cudaSuccess ? MPRES_SUCCESS : MPRES_ERR_CUDA;
+}
+
+int mpres_probe_latency(int which, long long iters, void *out, void *stream) {
+    if (which < 0 || which > 2 || iters <= 0 || !out) return MPRES_ERR_INVALID_VALUE;
+    probe_latency_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(which, iters, 1073741827u,
+                                                           (uint32_t)((1ull << 62) / 1073741827ull), (double *)out);
     return cudaGetLastError() == cudaSuccess ? MPRES_SUCCESS : MPRES_ERR_CUDA;
 }
 

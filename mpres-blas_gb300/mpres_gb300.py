@@ -58,6 +58,14 @@ _SIGS = {
     "mpres_ell_host2device": (I, [P, P, I, I]),
     "mpres_ell_clear": (I, [P]),
     "mpres_set_d": (I, [I, P, SZ, P]),
+    "mpres_div": (I, [I, P, P, P]),
+    "mpres_sqrt": (I, [I, P, P]),
+    "mpres_dsqrt": (I, [I, P, P]),
+    "mpres_div_device": (I, [I, P, P, P]),
+    "mpres_dsqrt_device": (I, [I, P, P]),
+    "mpres_mtx_stats": (I, [ctypes.c_char_p, P, P, P, P, P, P, P]),
+    "mpres_mtx_build_csr": (I, [ctypes.c_char_p, I, I, I, I, P, P, P]),
+    "mpres_mtx_build_ell": (I, [ctypes.c_char_p, I, I, I, I, P, P]),
     "mpres_set_d_device": (I, [I, P, SZ, P, P]),
     "mpres_array_set_d": (I, [I, P, SZ, P, SZ, P]),
     "mpres_dot": (I, [I, I, P, I, P, I, P, P, I, I, I, I, I, P]),
@@ -86,6 +94,7 @@ _SIGS = {
     "mpres_server_stats": (I, [P, P]),
     "mpres_probe_mulmod": (I, [I, I, ctypes.c_longlong, P, P]),
     "mpres_probe_dadd": (I, [I, I, ctypes.c_longlong, P, P]),
+    "mpres_probe_latency": (I, [I, ctypes.c_longlong, P, P]),
     "mpres_elementwise": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_ceil_log2": (I, [P, P, SZ, P]),
     "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
@@ -155,6 +164,58 @@ def array_set_d(nmod, arr, offset, x, stream=None):
 
 def mp_size(nmod):
     return 4 * nmod + 40
+
+
+def div(nmod, x, y):
+    """Host ::mp_div record by record (MPFR semantics at MP_PRECISION bits)."""
+    out = np.zeros(len(x), mp_dtype(nmod))
+    for i in range(len(x)):
+        check(lib().mpres_div(nmod, x[i:i + 1].ctypes.data, y[i:i + 1].ctypes.data, out[i:i + 1].ctypes.data),
+              "mpres_div")
+    return out
+
+
+def sqrt(nmod, x):
+    out = np.zeros(len(x), mp_dtype(nmod))
+    for i in range(len(x)):
+        check(lib().mpres_sqrt(nmod, x[i:i + 1].ctypes.data, out[i:i + 1].ctypes.data), "mpres_sqrt")
+    return out
+
+
+def dsqrt(nmod, x):
+    out = np.zeros(len(x))
+    for i in range(len(x)):
+        check(lib().mpres_dsqrt(nmod, x[i:i + 1].ctypes.data, out[i:i + 1].ctypes.data), "mpres_dsqrt")
+    return out
+
+
+def mtx_stats(path):
+    """collect_mtx_stats of a Matrix Market file."""
+    v = [ctypes.c_int() for _ in range(6)]
+    dt = ctypes.create_string_buffer(16)
+    check(lib().mpres_mtx_stats(str(path).encode(), *[ctypes.byref(x) for x in v], dt), "mpres_mtx_stats")
+    m, n, lines, maxnzr, nzmd, sym = (x.value for x in v)
+    nnz = 2 * (lines - nzmd) + nzmd if sym else lines
+    return dict(m=m, n=n, lines=lines, maxnzr=maxnzr, nzmd=nzmd, symmetric=sym, nnz=nnz, datatype=dt.value.decode())
+
+
+def mtx_csr(path, st=None):
+    """build_csr: (irp, ja, as) host arrays in the reference's entry order."""
+    st = st or mtx_stats(path)
+    irp, ja, vals = np.zeros(st["m"] + 1, np.int32), np.zeros(st["nnz"], np.int32), np.zeros(st["nnz"])
+    check(lib().mpres_mtx_build_csr(str(path).encode(), st["m"], st["nnz"], st["lines"], st["symmetric"],
+                                    vals.ctypes.data, ja.ctypes.data, irp.ctypes.data), "mpres_mtx_build_csr")
+    return irp, ja, vals
+
+
+def mtx_ell(path, st=None):
+    """build_ell: (ja, as) column-major m x maxnzr host arrays."""
+    st = st or mtx_stats(path)
+    size = st["m"] * st["maxnzr"]
+    ja, vals = np.zeros(size, np.int32), np.zeros(size)
+    check(lib().mpres_mtx_build_ell(str(path).encode(), st["m"], st["maxnzr"], st["lines"], st["symmetric"],
+                                    vals.ctypes.data, ja.ctypes.data), "mpres_mtx_build_ell")
+    return ja, vals
 
 
 def _stream_handle(stream):
@@ -542,7 +603,7 @@ def probe_check(which, nmod, a, b=None):
     a = np.ascontiguousarray(a)
     da = DeviceBytes.from_numpy(a)
     db = DeviceBytes.from_numpy(np.ascontiguousarray(b)) if b is not None else None
-    width, dt = {0: (4, np.float64), 1: (2, np.float64), 2: (2, np.int32)}[which]
+    width, dt = {0: (4, np.float64), 1: (2, np.float64), 2: (2, np.int32), 3: (2, np.int32)}[which]
     out = DeviceBytes(len(a) * width * np.dtype(dt).itemsize)
     check(lib().mpres_probe_check(which, nmod, da.ptr, db.ptr if db else None, out.ptr, len(a), None),
           "mpres_probe_check")

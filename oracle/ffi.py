@@ -167,6 +167,35 @@ def _tables(fn, n, log2m):
     return t
 
 
+def ref_div_sqrt(n, x, y):
+    """The reference's host ::mp_div(x, y), ::mp_sqrt(|x|) and ::mp_dsqrt(|x|) (MPFR)."""
+    lib = reference(n).lib
+    cnt = len(x)
+    q, r, d = np.zeros(cnt, mp_dtype(n)), np.zeros(cnt, mp_dtype(n)), np.zeros(cnt)
+    ax = x.copy()
+    ax["sign"] = 0
+    lib.ref_div(ptr(x), ptr(y), ptr(q), ctypes.c_long(cnt))
+    lib.ref_sqrt(ptr(ax), ptr(r), ctypes.c_long(cnt))
+    lib.ref_dsqrt(ptr(ax), ptr(d), ctypes.c_long(cnt))
+    return q, r, d
+
+
+def ref_mtx(n, path):
+    """The reference's Matrix Market reader (collect_mtx_stats, build_csr,
+    build_ell) on a file: stats, (irp, ja, as), (ell ja, ell as)."""
+    lib = reference(n).lib
+    st = np.zeros(6, np.int32)
+    b = str(path).encode()
+    lib.ref_mtx_stats(b, ptr(st))
+    m, cols, lines, maxnzr, nzmd, sym = (int(v) for v in st)
+    nnz = 2 * (lines - nzmd) + nzmd if sym else lines
+    irp, ja, vals = np.zeros(m + 1, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz, np.float64)
+    lib.ref_mtx_csr(b, m, nnz, lines, sym, ptr(vals), ptr(ja), ptr(irp))
+    eja, eas = np.zeros(m * maxnzr, np.int32), np.zeros(m * maxnzr, np.float64)
+    lib.ref_mtx_ell(b, m, maxnzr, lines, sym, ptr(eas), ptr(eja))
+    return dict(m=m, n=cols, lines=lines, maxnzr=maxnzr, nzmd=nzmd, symmetric=sym), (irp, ja, vals), (eja, eas)
+
+
 _refs = {}
 
 

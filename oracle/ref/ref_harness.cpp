@@ -20,6 +20,8 @@
 #include "arith/add.cuh"
 #include "arith/mul.cuh"
 #include "arith/muld.cuh"
+#include "arith/div.cuh"
+#include "arith/sqrt.cuh"
 #include "mpvector.cuh"
 #include "mpmatrix.cuh"
 #include "mpreduct.cuh"
@@ -28,6 +30,7 @@
 #include "sparse/spmv/spmv_csr.cuh"
 #include "sparse/spmv/spmv_csrv.cuh"
 #include "sparse/spmv/spmv_ell.cuh"
+#include "sparse/utils/mtx_reader.cuh"
 
 uint3 threadIdx, blockIdx;
 dim3 blockDim, gridDim;
@@ -343,6 +346,47 @@ void ref_spmv_ell(int m, int maxnzr, const int *ja, const double *as, const mp_f
     ell.ja = (int *)ja; ell.as = (double *)as;
     mp_float_ptr px = (mp_float_ptr)x;
     emu::launch(dim3(m / 32 + 1), dim3(32), [&] { cuda::mp_spmv_ell<32>(m, maxnzr, ell, px, y); }, false);
+}
+
+/* ::mp_div, ::mp_sqrt, ::mp_dsqrt (src/arith/div.cuh:33-45, src/arith/sqrt.cuh),
+ * host functions on MPFR, called as written, element by element. */
+void ref_div(const mp_float_t *x, const mp_float_t *y, mp_float_t *r, long count) {
+    for (long i = 0; i < count; i++) {
+        mp_float_t a = x[i], b = y[i];
+        ::mp_div(&r[i], &a, &b);
+    }
+}
+void ref_sqrt(const mp_float_t *x, mp_float_t *r, long count) {
+    for (long i = 0; i < count; i++) {
+        mp_float_t a = x[i];
+        ::mp_sqrt(&r[i], &a);
+    }
+}
+void ref_dsqrt(const mp_float_t *x, double *r, long count) {
+    for (long i = 0; i < count; i++) {
+        mp_float_t a = x[i];
+        r[i] = ::mp_dsqrt(&a);
+    }
+}
+
+/* The Matrix Market reader, src/sparse/utils/mtx_reader.cuh:52-101, :249-253,
+ * :374-406, called as written.  out = {m, n, lines, maxnzr, nzmd, symmetric}. */
+void ref_mtx_stats(const char *path, int *out) {
+    int m, n, lines, maxnzr, nzmd;
+    bool sym;
+    std::string dtype;
+    collect_mtx_stats(path, m, n, lines, maxnzr, nzmd, sym, dtype);
+    out[0] = m; out[1] = n; out[2] = lines; out[3] = maxnzr; out[4] = nzmd; out[5] = sym;
+}
+void ref_mtx_csr(const char *path, int m, int nnz, int lines, int symmetric, double *as, int *ja, int *irp) {
+    csr_t csr;
+    csr.as = as; csr.ja = ja; csr.irp = irp;
+    build_csr(path, m, nnz, lines, symmetric != 0, csr);
+}
+void ref_mtx_ell(const char *path, int m, int maxnzr, int lines, int symmetric, double *as, int *ja) {
+    ell_t ell;
+    ell.as = as; ell.ja = ja;
+    build_ell(path, m, maxnzr, lines, symmetric != 0, ell);
 }
 
 } // extern "C"

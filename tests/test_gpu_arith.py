@@ -127,3 +127,26 @@ def test_fixed_point_ceil_log2_matches_cuda(gpu):
     out = gpu.probe_check(2, 8, x)
     bad = np.nonzero(out[:, 0] != out[:, 1])[0]
     assert len(bad) == 0, [(float.hex(float(x[i])), out[i].tolist()) for i in bad[:5]]
+
+
+def test_ceil_log2_of_doubles_matches_cuda(gpu):
+    """ceil(log2(x)) from the bits of any positive double (normal and subnormal,
+    at, just above and just below every power of two) equals CUDA's."""
+    rng = np.random.default_rng(helpers.SEED + 951)
+    powers = np.ldexp(1.0, np.arange(-1074, 1024))
+    near = [powers]
+    x = powers
+    for k in range(1, 40):
+        near.append(np.nextafter(x, np.inf))
+        x = near[-1]
+    x = powers
+    for k in range(1, 40):
+        x = np.nextafter(x, 0)
+        near.append(x)
+    wild = np.abs(_doubles_all_binades(rng, 400000))
+    allx = np.concatenate(near + [wild, np.ldexp(1.0 + np.arange(1, 5000) * 2.0 ** -52, -60),
+                                  np.ldexp(2.0 - np.arange(1, 5000) * 2.0 ** -52, -61)])
+    allx = allx[(allx > 0) & np.isfinite(allx)]
+    out = gpu.probe_check(3, 8, allx)
+    bad = np.nonzero(out[:, 0] != out[:, 1])[0]
+    assert len(bad) == 0, [(float.hex(float(allx[i])), out[i].tolist()) for i in bad[:5]]

@@ -251,3 +251,25 @@ def test_bad_arguments_are_reported(gpu):
     with pytest.raises(gpu.MpresError):
         gpu.spmv_csrv(8, 2, c, x, x, tpr=3)
     assert gpu.lib().mpres_dot(12, 4, d.ref, 1, d.ref, 1, d.ref, None, 1, 1, 1, 1, 1, None) != 0
+
+
+# ------------------------------------------------------ Matrix Market input ----
+
+def test_spmv_from_matrix_market_file(gpu, oracle, tmp_path):
+    """A symmetric file read by the library's reader: CSR, CSR-vector and ELL
+    results on the GPU equal the oracle's on the same arrays."""
+    import test_mtx
+    rng = np.random.default_rng(helpers.SEED + 61)
+    ent = test_mtx.random_entries(rng, 5000, 5000, 30000, symmetric=True)
+    ent += [(i, i, rng.normal()) for i in range(1, 5001, 2)]
+    rng.shuffle(ent)
+    path = test_mtx.write_mtx(tmp_path / "sym.mtx", 5000, 5000, ent, symmetric=True)
+    st = gpu.mtx_stats(path)
+    irp, ja, vals = gpu.mtx_csr(path, st)
+    eja, eas = gpu.mtx_ell(path, st)
+    m = st["m"]
+    mx = gpu.set_d(8, helpers.doubles(rng, m, -16, 16))
+    eq(run_spmv(gpu, 8, "csr", m, mx, irp, ja, vals), oracle.spmv_csr(8, m, irp, ja, vals, mx))
+    eq(run_spmv(gpu, 8, "csrv", m, mx, irp, ja, vals, tpr=8), oracle.spmv_csrv(8, m, 8, irp, ja, vals, mx))
+    eq(run_spmv(gpu, 8, "ell", m, mx, maxnzr=st["maxnzr"], ell_ja=eja, ell_as=eas),
+       oracle.spmv_ell(8, m, st["maxnzr"], eja, eas, mx))
