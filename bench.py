@@ -319,7 +319,7 @@ def same(a, snap):
     return all(torch.equal(t, v) for t, v in zip((a.digits, a.sign, a.exp, a.eval), snap))
 
 
-def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=40 << 30):
+def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
     """4096 mp_gemv y = alpha*A*x + beta*y (NO_TRANS, lda = m), m and n
     log-uniform in [32, 4096], entries u*2^e with e in [-32, 32], 16 moduli:
     one persistent launch per wave (graph replay, autotuned shape) against the

@@ -152,6 +152,43 @@ int mpres_set_d(int nmod, const double *x, size_t count, void *out);
 int mpres_set_d_device(int nmod, const double *x, size_t count, void *out, void *stream);
 int mpres_array_set_d(int nmod, mp_array_t *dst, size_t offset, const double *x, size_t count, void *stream);
 
+/* ---- v2 vector kernels over AoS mp_float_t vectors (device memory) -------- */
+
+/* cuda::mp_diff (src/blas/v2/diff_v2.cuh): r = x - y;
+ * cuda::mp_axpy (axpy_v2.cuh): r = alpha*x + y;  cuda::mp_maxpy (maxpy_v2.cuh):
+ * r = -alpha*x + y (alpha a device record).  The reference's kernels are launched
+ * by their callers with <<<n/threads + 1, threads>>>; element-wise results do
+ * not depend on the launch. */
+int mpres_v2_diff(int nmod, int n, const void *x, const void *y, void *r, int threads, void *stream);
+int mpres_v2_axpy(int nmod, int n, const void *alpha, const void *x, const void *y, void *r, int threads,
+                  void *stream);
+int mpres_v2_maxpy(int nmod, int n, const void *alpha, const void *x, const void *y, void *r, int threads,
+                   void *stream);
+/* cuda::mp_dot<blocks, threads> (dot_v2.cuh): r[0] = x.y, blocks*threads strided
+ * chains, a tree per block, one block over the block sums (the order is the
+ * reference's for the same blocks and threads, threads <= 256). */
+int mpres_v2_dot(int nmod, int n, const void *x, const void *y, void *r, int blocks, int threads, void *stream);
+/* cuda::mp_norm2<blocks, threads> (norm2_v2.cuh): the sum of squares with
+ * mp_add_abs in the same two-pass order, then mp_dsqrt on the host; waits for
+ * the stream. */
+int mpres_v2_norm2(int nmod, int n, const void *x, double *out, int blocks, int threads, void *stream);
+
+/* ---- conjugate gradients over CSR ---------------------------------------- */
+
+/* mp_cg_csr<threads, blocks_reduce> (src/sparse/solver/cg_csr.cuh) and
+ * mp_pcg_csr (pcg_csr.cuh, Jacobi preconditioner: ptype 1, M = the inverse
+ * diagonal as doubles in device memory): solves A x = b for a double CSR matrix
+ * A (device) with AoS mp_float_t vectors b and x (device; x holds the initial
+ * guess and receives the solution).  resvec (host, resvec_cap doubles)
+ * receives ||r_k|| / ||r_0|| for k = 0..iters, as the reference's resvec;
+ * *iters the iterations run.  Bit-identical to the reference for the same
+ * threads and blocks_reduce (32 and 256 in cg_csr.cuh, 64 and 256 in
+ * pcg_csr.cuh).  Synchronous: the divisions run on the host each iteration. */
+int mpres_cg_csr(int nmod, int n, const csr_t *A, const void *b, double tol, int maxit, void *x, double *resvec,
+                 int resvec_cap, int *iters, int threads, int blocks_reduce, void *stream);
+int mpres_pcg_csr(int nmod, int n, const csr_t *A, const void *b, double tol, int maxit, int ptype, const double *M,
+                  void *x, double *resvec, int resvec_cap, int *iters, int threads, int blocks_reduce, void *stream);
+
 /* ---- host MPFR operations ------------------------------------------------ */
 
 /* ::mp_div (src/arith/div.cuh:33-45), ::mp_sqrt and ::mp_dsqrt (src/arith/sqrt.cuh):

@@ -16,6 +16,11 @@
  *   cuda::ell_init/ell_host2device/ell_clear          src/sparse/utils/ell_utils.cuh:55-71
  *   cuda::mp_spmv_csr<threads>, mp_spmv_csrv<threads,tpr>, mp_spmv_ell<threads>
  *                                                     src/sparse/spmv/spmv_{csr,csrv,ell}.cuh
+ *   cuda::mp_diff/mp_axpy/mp_maxpy, cuda::mp_dot<blocks,threads>, cuda::mp_norm2<blocks,threads>
+ *                                                     src/blas/v2/{diff,axpy,maxpy,dot,norm2}_v2.cuh
+ *   mp_cg_csr<threads,blocks>, mp_pcg_csr<threads,blocks>  src/sparse/solver/{cg,pcg}_csr.cuh
+ *   ::mp_div, ::mp_sqrt, ::mp_dsqrt, cuda::mp_div, cuda::mp_dsqrt  src/arith/{div,sqrt}.cuh
+ *   collect_mtx_stats, build_csr, build_ell           src/sparse/utils/mtx_reader.cuh
  *
  * The reference's SpMV routines are kernels the caller launches with
  * <<<blocks, threads>>>; here they are host functions taking the same
@@ -29,6 +34,7 @@
 
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "mpres_gb300.h"
 
@@ -132,7 +138,75 @@ template <int threads> void mp_spmv_ell(const int m, const int maxnzr, const ell
     mpres_detail::report(mpres_spmv_ell(RNS_MODULI_SIZE, m, maxnzr, &ell, x, y, threads, nullptr), "mp_spmv_ell");
 }
 
+/* v2 vector kernels (src/blas/v2/*_v2.cuh): host functions with the kernels' arguments */
+inline void mp_diff(const int n, mp_float_ptr x, mp_float_ptr y, mp_float_ptr r) {
+    mpres_detail::report(mpres_v2_diff(RNS_MODULI_SIZE, n, x, y, r, 32, nullptr), "mp_diff");
+}
+inline void mp_axpy(const int n, mp_float_ptr alpha, mp_float_ptr x, mp_float_ptr y, mp_float_ptr r) {
+    mpres_detail::report(mpres_v2_axpy(RNS_MODULI_SIZE, n, alpha, x, y, r, 32, nullptr), "mp_axpy");
+}
+inline void mp_maxpy(const int n, mp_float_ptr alpha, mp_float_ptr x, mp_float_ptr y, mp_float_ptr r) {
+    mpres_detail::report(mpres_v2_maxpy(RNS_MODULI_SIZE, n, alpha, x, y, r, 32, nullptr), "mp_maxpy");
+}
+template <int blocks, int threads> void mp_dot(const int n, mp_float_ptr x, mp_float_ptr y, mp_float_ptr r) {
+    mpres_detail::report(mpres_v2_dot(RNS_MODULI_SIZE, n, x, y, r, blocks, threads, nullptr), "mp_dot");
+}
+template <int blocks, int threads> double mp_norm2(const int n, mp_float_ptr x) {
+    double v = 0;
+    mpres_detail::report(mpres_v2_norm2(RNS_MODULI_SIZE, n, x, &v, blocks, threads, nullptr), "mp_norm2");
+    return v;
+}
+/* src/arith/div.cuh:56-65, src/arith/sqrt.cuh: device records, host computation */
+inline void mp_div(mp_float_ptr result, mp_float_ptr x, mp_float_ptr y) {
+    mpres_detail::report(mpres_div_device(RNS_MODULI_SIZE, x, y, result), "mp_div");
+}
+inline double mp_dsqrt(mp_float_ptr x) {
+    double v = 0;
+    mpres_detail::report(mpres_dsqrt_device(RNS_MODULI_SIZE, x, &v), "mp_dsqrt");
+    return v;
+}
+
 } // namespace cuda
+
+/* host MPFR operations (src/arith/div.cuh:33-45, src/arith/sqrt.cuh) */
+inline void mp_div(mp_float_ptr result, mp_float_ptr x, mp_float_ptr y) {
+    mpres_detail::report(mpres_div(RNS_MODULI_SIZE, x, y, result), "mp_div");
+}
+inline void mp_sqrt(mp_float_ptr result, mp_float_ptr x) {
+    mpres_detail::report(mpres_sqrt(RNS_MODULI_SIZE, x, result), "mp_sqrt");
+}
+inline double mp_dsqrt(mp_float_ptr x) {
+    double v = 0;
+    mpres_detail::report(mpres_dsqrt(RNS_MODULI_SIZE, x, &v), "mp_dsqrt");
+    return v;
+}
+
+/* conjugate gradients (src/sparse/solver/cg_csr.cuh, pcg_csr.cuh); resvec is
+ * appended to, as in the reference */
+#ifndef MPRES_MSPARSE_ENUM_CUH
+#define MPRES_MSPARSE_ENUM_CUH
+enum preconditioner_type { diag = 1 };
+#endif
+template <int threads = 32, int blocks_reduce = 256>
+int mp_cg_csr(const int n, const csr_t &A, mp_float_ptr b, const double tol, const int maxit, mp_float_ptr x,
+              std::vector<double> &resvec) {
+    std::vector<double> res((size_t)maxit + 1);
+    int k = 0;
+    mpres_detail::report(mpres_cg_csr(RNS_MODULI_SIZE, n, &A, b, tol, maxit, x, res.data(), (int)res.size(), &k,
+                                      threads, blocks_reduce, nullptr), "mp_cg_csr");
+    resvec.insert(resvec.end(), res.begin(), res.begin() + k + 1);
+    return k;
+}
+template <int threads = 64, int blocks_reduce = 256>
+int mp_pcg_csr(const int n, const csr_t &A, mp_float_ptr b, const double tol, const int maxit,
+               enum preconditioner_type ptype, double *M, mp_float_ptr x, std::vector<double> &resvec) {
+    std::vector<double> res((size_t)maxit + 1);
+    int k = 0;
+    mpres_detail::report(mpres_pcg_csr(RNS_MODULI_SIZE, n, &A, b, tol, maxit, (int)ptype, M, x, res.data(),
+                                       (int)res.size(), &k, threads, blocks_reduce, nullptr), "mp_pcg_csr");
+    resvec.insert(resvec.end(), res.begin(), res.begin() + k + 1);
+    return k;
+}
 
 /* src/sparse/utils/mtx_reader.cuh:52, :249, :374 (global functions in the reference) */
 inline void collect_mtx_stats(const char *filename, int &m, int &n, int &lines, int &maxnzr, int &nzmd,

@@ -131,6 +131,7 @@ cudaError_t upload_all(const HostTables &h, const int *dpow2, const int *dpow2_i
     if ((e = upload_tables_elementwise(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_convert(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_batch(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_solver(N, &t)) != cudaSuccess) return e;
     return upload_tables_spmv(N, &t);
 }
 
@@ -470,6 +471,97 @@ int mpres_dsqrt_device(int nmod, const void *x, double *out) {
     if (e != cudaSuccess) return cuda_fail(e, "mpres_dsqrt_device");
     if (!host_mp_dsqrt(*t, a, *out)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_dsqrt_device: negative operand");
     return ok();
+}
+
+/* ---- v2 vector kernels and conjugate gradients ---- */
+
+static int v2_threads(int threads, const char *what) {
+    if (threads < 1 || threads > 256)
+        return status_fail(MPRES_ERR_INVALID_VALUE, "%s: threads %d out of range (1..256)", what, threads);
+    return MPRES_SUCCESS;
+}
+
+static int v2_vec(const char *what, int nmod, int op, int n, const void *alpha, const void *x, const void *y, void *r,
+                  int threads, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (n <= 0) return ok();
+    if (!x || !y || !r || (op != 0 && !alpha)) return fail(MPRES_ERR_INVALID_VALUE, "%s: null argument", what);
+    if (int st = v2_threads(threads, what)) return st;
+    cudaError_t e = launch_vec_v2(nmod, op, n, threads, alpha, x, y, r, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, what);
+}
+
+int mpres_v2_diff(int nmod, int n, const void *x, const void *y, void *r, int threads, void *stream) {
+    return v2_vec("mpres_v2_diff", nmod, 0, n, nullptr, x, y, r, threads, stream);
+}
+int mpres_v2_axpy(int nmod, int n, const void *alpha, const void *x, const void *y, void *r, int threads,
+                  void *stream) {
+    return v2_vec("mpres_v2_axpy", nmod, 1, n, alpha, x, y, r, threads, stream);
+}
+int mpres_v2_maxpy(int nmod, int n, const void *alpha, const void *x, const void *y, void *r, int threads,
+                   void *stream) {
+    return v2_vec("mpres_v2_maxpy", nmod, 2, n, alpha, x, y, r, threads, stream);
+}
+
+int mpres_v2_dot(int nmod, int n, const void *x, const void *y, void *r, int blocks, int threads, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (n <= 0) return ok();
+    if (!x || !y || !r) return fail(MPRES_ERR_INVALID_VALUE, "mpres_v2_dot: null argument");
+    if (int st = v2_threads(threads, "mpres_v2_dot")) return st;
+    if (blocks < 1) return fail(MPRES_ERR_INVALID_VALUE, "mpres_v2_dot: blocks %d", blocks);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, (size_t)blocks * mp_size(nmod), ws)) return st;
+    cudaError_t e = launch_reduce_v2(nmod, false, n, blocks, threads, x, y, ws.ptr, r, s);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_v2_dot");
+}
+
+int mpres_v2_norm2(int nmod, int n, const void *x, double *out, int blocks, int threads, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (!x || !out) return fail(MPRES_ERR_INVALID_VALUE, "mpres_v2_norm2: null argument");
+    if (int st = v2_threads(threads, "mpres_v2_norm2")) return st;
+    if (blocks < 1) return fail(MPRES_ERR_INVALID_VALUE, "mpres_v2_norm2: blocks %d", blocks);
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, "mpres_v2_norm2", t)) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, (size_t)(blocks + 1) * mp_size(nmod), ws)) return st;
+    char *parts = static_cast<char *>(ws.ptr), *sum = parts + (size_t)blocks * mp_size(nmod);
+    cudaError_t e = launch_reduce_v2(nmod, true, n > 0 ? n : 0, blocks, threads, x, x, parts, sum, s);
+    char h[168];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, sum, mp_size(nmod), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "mpres_v2_norm2");
+    if (!host_mp_dsqrt(*t, h, *out)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_v2_norm2: negative sum");
+    return ok();
+}
+
+static int cg_common(const char *what, int nmod, int n, const csr_t *A, const void *b, double tol, int maxit,
+                     const double *M, void *x, double *resvec, int resvec_cap, int *iters, int threads,
+                     int blocks_reduce, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (n <= 0 || !A || !b || !x || (resvec_cap > 0 && !resvec))
+        return fail(MPRES_ERR_INVALID_VALUE, "%s: bad arguments", what);
+    if (int st = v2_threads(threads, what)) return st;
+    if (blocks_reduce < 1) return fail(MPRES_ERR_INVALID_VALUE, "%s: blocks_reduce %d", what, blocks_reduce);
+    const HostTables *t;
+    if (int st = host_tables_of(nmod, what, t)) return st;
+    return solve_cg(nmod, *t, n, *A, b, tol, maxit, M, x, resvec, resvec_cap, iters, threads, blocks_reduce,
+                    static_cast<cudaStream_t>(stream));
+}
+
+int mpres_cg_csr(int nmod, int n, const csr_t *A, const void *b, double tol, int maxit, void *x, double *resvec,
+                 int resvec_cap, int *iters, int threads, int blocks_reduce, void *stream) {
+    return cg_common("mpres_cg_csr", nmod, n, A, b, tol, maxit, nullptr, x, resvec, resvec_cap, iters, threads,
+                     blocks_reduce, stream);
+}
+
+int mpres_pcg_csr(int nmod, int n, const csr_t *A, const void *b, double tol, int maxit, int ptype, const double *M,
+                  void *x, double *resvec, int resvec_cap, int *iters, int threads, int blocks_reduce, void *stream) {
+    if (ptype != 1 || !M)
+        return fail(MPRES_ERR_NOT_SUPPORTED, "mpres_pcg_csr: only the diagonal (Jacobi) preconditioner, ptype 1");
+    return cg_common("mpres_pcg_csr", nmod, n, A, b, tol, maxit, M, x, resvec, resvec_cap, iters, threads,
+                     blocks_reduce, stream);
 }
 
 int mpres_set_d(int nmod, const double *x, size_t count, void *out) {

@@ -19,6 +19,7 @@ cudaError_t upload_tables_spmv(int n, const void *tab);
 cudaError_t upload_tables_elementwise(int n, const void *tab);
 cudaError_t upload_tables_convert(int n, const void *tab);
 cudaError_t upload_tables_batch(int n, const void *tab);
+cudaError_t upload_tables_solver(int n, const void *tab);
 
 /* Scratch for one call, carved from a per-device workspace. */
 struct Workspace {
@@ -69,6 +70,17 @@ cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void
                          cudaStream_t s);
 cudaError_t launch_eval(int nmod, int fast, const int *digits, er_t *low, er_t *upp, long long count,
                         cudaStream_t s);
+
+/* conjugate gradients and the v2 vector kernels (solver.cu); M == nullptr: plain CG */
+int solve_cg(int nmod, const HostTables &t, int n, const csr_t &A, const void *b, double tol, int maxit,
+             const double *M, void *x, double *resvec, int resvec_cap, int *iters, int threads, int blocks_reduce,
+             cudaStream_t s);
+/* op 0: r = x - y, 1: r = alpha x + y, 2: r = -alpha x + y (AoS records) */
+cudaError_t launch_vec_v2(int nmod, int op, int n, int threads, const void *alpha, const void *x, const void *y,
+                          void *r, cudaStream_t s);
+/* r[0] = x.y (sumsq: sum of |x_i^2| with mp_add_abs); parts holds `blocks` records */
+cudaError_t launch_reduce_v2(int nmod, bool sumsq, int n, int blocks, int threads, const void *x, const void *y,
+                             void *parts, void *r, cudaStream_t s);
 
 /* status reporting shared by the C entry points (capi.cu): set the thread's
  * last-error text and return the status */

@@ -611,6 +611,41 @@ template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N
     round_if_needed<N>(r);
 }
 
+/* cuda::mp_add_abs: |x| + |y|, mp_add_abs_common (src/arith/addabs.cuh:81-127):
+ * the aligned residues added with 0/1 factors, no signs, bounds added as stored */
+template <int N> __device__ __forceinline__ void mp_add_abs(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y) {
+    const Tables<N> &t = T<N>();
+    int ex = x.exp, ey = y.exp;
+    const int dexp = ex - ey;
+    int gamma = dexp > 0 ? dexp : 0;
+    int theta = dexp < 0 ? -dexp : 0;
+    const int nzx = (!dnz(y.ev[1].frac) || (theta + y.ev[1].exp) < t.mp_j);
+    const int nzy = (!dnz(x.ev[1].frac) || (gamma + x.ev[1].exp) < t.mp_j);
+    gamma *= nzy;
+    theta *= nzx;
+    ex = (ex - gamma) * nzx;
+    ey = (ey - theta) * nzy;
+    r.exp = (ex == 0) ? ey : ex;
+    r.sign = 0;
+    er_t ax[2], ay[2];
+    ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
+    ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
+    ax[0].frac = dscale_sign(x.ev[0].frac, nzx); ax[1].frac = dscale_sign(x.ev[1].frac, nzx);
+    ay[0].frac = dscale_sign(y.ev[0].frac, nzy); ay[1].frac = dscale_sign(y.ev[1].frac, nzy);
+    r.ev[0] = er_add<false>(ax[0], ay[0]);
+    r.ev[1] = er_add<true>(ax[1], ay[1]);
+    const int *pg = t.pow2 + (size_t)pow2_row_index<N>(gamma) * N;
+    const int *pt = t.pow2 + (size_t)pow2_row_index<N>(theta) * N;
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i];
+        const uint32_t u = nzx ? mulmod((uint32_t)__ldg(pg + i), (uint32_t)x.d[i], m, t.mu[i]) : 0u;
+        const uint32_t v = nzy ? mulmod((uint32_t)__ldg(pt + i), (uint32_t)y.d[i], m, t.mu[i]) : 0u;
+        r.d[i] = (int)reduce2(u + v, m);
+    }
+    round_if_needed<N>(r);
+}
+
 /* cuda::mp_mul: mp_mul_common + rounding (src/arith/mul.cuh:53-113); also the
  * split kernels mp_*_mul_esi/digits + round of src/mpvector.cuh, src/mpmatrix.cuh */
 template <int N> __device__ __forceinline__ void mp_mul(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y) {

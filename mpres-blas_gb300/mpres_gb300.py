@@ -58,6 +58,13 @@ _SIGS = {
     "mpres_ell_host2device": (I, [P, P, I, I]),
     "mpres_ell_clear": (I, [P]),
     "mpres_set_d": (I, [I, P, SZ, P]),
+    "mpres_v2_diff": (I, [I, I, P, P, P, I, P]),
+    "mpres_v2_axpy": (I, [I, I, P, P, P, P, I, P]),
+    "mpres_v2_maxpy": (I, [I, I, P, P, P, P, I, P]),
+    "mpres_v2_dot": (I, [I, I, P, P, P, I, I, P]),
+    "mpres_v2_norm2": (I, [I, I, P, P, I, I, P]),
+    "mpres_cg_csr": (I, [I, I, P, P, ctypes.c_double, I, P, P, I, P, I, I, P]),
+    "mpres_pcg_csr": (I, [I, I, P, P, ctypes.c_double, I, I, P, P, P, I, P, I, I, P]),
     "mpres_div": (I, [I, P, P, P]),
     "mpres_sqrt": (I, [I, P, P]),
     "mpres_dsqrt": (I, [I, P, P]),
@@ -164,6 +171,44 @@ def array_set_d(nmod, arr, offset, x, stream=None):
 
 def mp_size(nmod):
     return 4 * nmod + 40
+
+
+def v2_vec(nmod, op, n, x, y, r, alpha=None, threads=32, stream=None):
+    """op "diff": r = x - y; "axpy": r = alpha x + y; "maxpy": r = -alpha x + y (DeviceBytes records)."""
+    h = _stream_handle(stream)
+    if op == "diff":
+        check(lib().mpres_v2_diff(nmod, n, x.ptr, y.ptr, r.ptr, threads, h), "mpres_v2_diff")
+    else:
+        f = lib().mpres_v2_axpy if op == "axpy" else lib().mpres_v2_maxpy
+        check(f(nmod, n, alpha.ptr, x.ptr, y.ptr, r.ptr, threads, h), "mpres_v2_" + op)
+
+
+def v2_dot(nmod, n, x, y, r, blocks=256, threads=32, stream=None):
+    check(lib().mpres_v2_dot(nmod, n, x.ptr, y.ptr, r.ptr, blocks, threads, _stream_handle(stream)), "mpres_v2_dot")
+
+
+def v2_norm2(nmod, n, x, blocks=256, threads=32, stream=None):
+    out = ctypes.c_double()
+    check(lib().mpres_v2_norm2(nmod, n, x.ptr, ctypes.byref(out), blocks, threads, _stream_handle(stream)),
+          "mpres_v2_norm2")
+    return out.value
+
+
+def cg_csr(nmod, n, csr, b, x, tol, maxit, M=None, threads=None, blocks=256, stream=None):
+    """mp_cg_csr (M None) / mp_pcg_csr (M: DeviceBytes of n doubles, the inverse
+    diagonal): x (DeviceBytes records) is the guess and the solution; returns
+    (iterations, resvec)."""
+    res = np.zeros(maxit + 2)
+    k = ctypes.c_int()
+    h = _stream_handle(stream)
+    if M is None:
+        check(lib().mpres_cg_csr(nmod, n, ctypes.byref(csr.c), b.ptr, tol, maxit, x.ptr, res.ctypes.data, len(res),
+                                 ctypes.byref(k), threads or 32, blocks, h), "mpres_cg_csr")
+    else:
+        check(lib().mpres_pcg_csr(nmod, n, ctypes.byref(csr.c), b.ptr, tol, maxit, 1, M.ptr, x.ptr,
+                                  res.ctypes.data, len(res), ctypes.byref(k), threads or 64, blocks, h),
+              "mpres_pcg_csr")
+    return k.value, res[: k.value + 1]
 
 
 def div(nmod, x, y):

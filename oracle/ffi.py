@@ -116,6 +116,16 @@ class Oracle(_Common):
         self.lib.ora_scale2pow(n, ptr(digits), ptr(D), ptr(out), ctypes.c_long(D.size))
         return out
 
+    def add_abs(self, n, x, y):
+        r = np.zeros(len(x), mp_dtype(n))
+        self.lib.ora_add_abs(n, ptr(x), ptr(y), ptr(r), ctypes.c_long(len(x)))
+        return r
+
+    def reduce_v2(self, n, sumsq, x, y, blocks, threads):
+        r = np.zeros(1, mp_dtype(n))
+        self.lib.ora_reduce_v2(n, int(sumsq), len(x), ptr(x), ptr(y if y is not None else x), ptr(r), blocks, threads)
+        return r
+
     def dot(self, n, x, y, g3=256, b3=64, incx=1, incy=1, length=None):
         length = len(x) if length is None else length
         r = np.zeros(1, mp_dtype(n))
@@ -165,6 +175,33 @@ def _tables(fn, n, log2m):
     )
     fn(*[ptr(v) for v in t.values()])
     return t
+
+
+def ref_add_abs(n, x, y):
+    r = np.zeros(len(x), mp_dtype(n))
+    reference(n).lib.ref_add_abs(ptr(x), ptr(y), ptr(r), ctypes.c_long(len(x)))
+    return r
+
+
+def ref_reduce_v2(n, sumsq, x, y, blocks, threads):
+    r = np.zeros(1, mp_dtype(n))
+    reference(n).lib.ref_reduce_v2(int(sumsq), len(x), ptr(x), ptr(y if y is not None else x), ptr(r), blocks, threads)
+    return r
+
+
+def ref_cg(n, irp, ja, vals, b, tol, maxit, x0, M=None, threads=32, blocks=256):
+    """The reference's mp_cg_csr (M None) or mp_pcg_csr (M = inverse diagonal):
+    (iterations, x, resvec)."""
+    x = x0.copy()
+    res = np.zeros(maxit + 2)
+    irp, ja = np.ascontiguousarray(irp, np.int32), np.ascontiguousarray(ja, np.int32)
+    vals = np.ascontiguousarray(vals, np.float64)
+    Mp = ptr(np.ascontiguousarray(M, np.float64)) if M is not None else None
+    lib = reference(n).lib
+    lib.ref_cg_csr.restype = ctypes.c_int
+    k = lib.ref_cg_csr(len(b), ptr(irp), ptr(ja), ptr(vals), ptr(b), ctypes.c_double(tol), maxit, Mp, ptr(x),
+                       ptr(res), len(res), threads, blocks)
+    return k, x, res[: k + 1]
 
 
 def ref_div_sqrt(n, x, y):

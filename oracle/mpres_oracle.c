@@ -786,6 +786,44 @@ static void mp_add(const ora_ctx_t *c, mpf_t *r, const mpf_t *xin, const mpf_t *
     *r = out;
 }
 
+/* src/arith/addabs.cuh:81-127 (cuda::mp_add_abs_common + rounding): |x| + |y| */
+static void mp_add_abs(const ora_ctx_t *c, mpf_t *r, const mpf_t *xin, const mpf_t *yin) {
+    const int n = c->n;
+    mpf_t x = *xin, y = *yin;
+    int ex = x.exp, ey = y.exp;
+    er_t *evalx = x.eval, *evaly = y.eval;
+    int dexp = ex - ey;
+    int gamma = dexp * (dexp > 0);
+    int theta = -dexp * (dexp < 0);
+    const int nzx = ((evaly[1].frac == 0) || (theta + evaly[1].exp) < c->mp_j);
+    const int nzy = ((evalx[1].frac == 0) || (gamma + evalx[1].exp) < c->mp_j);
+    gamma = gamma * nzy;
+    theta = theta * nzx;
+    ex = (ex - gamma) * nzx;
+    ey = (ey - theta) * nzy;
+    mpf_t out;
+    out.exp = (ex == 0) ? ey : ex;
+    out.sign = 0;
+    evalx[0].exp += gamma;
+    evalx[1].exp += gamma;
+    evaly[0].exp += theta;
+    evaly[1].exp += theta;
+    evalx[0].frac *= nzx;
+    evalx[1].frac *= nzx;
+    evaly[0].frac *= nzy;
+    evaly[1].frac *= nzy;
+    out.eval[0] = er_add_dir(evalx[0], evaly[0], 0);
+    out.eval[1] = er_add_dir(evalx[1], evaly[1], 1);
+    const int *pg = &c->pow2[pow2_row(c, gamma) * n], *pt = &c->pow2[pow2_row(c, theta) * n];
+    for (int i = 0; i < n; i++) {
+        int64_t res = (int64_t)pg[i] * (int64_t)x.digits[i] * (int64_t)nzx + (int64_t)pt[i] * (int64_t)y.digits[i] * (int64_t)nzy;
+        res = res % (int64_t)c->moduli[i];
+        out.digits[i] = (int)res + (res < 0) * c->moduli[i];
+    }
+    mp_round_if_needed(c, &out);
+    *r = out;
+}
+
 /* src/arith/mul.cuh:53-113 (cuda::mp_mul_common + rounding); the split kernels
  * mp_vector_mul_esi/digits_kernel + mp_vector_round_kernel compute the same. */
 static void mp_mul(const ora_ctx_t *c, mpf_t *r, const mpf_t *x, const mpf_t *y) {
@@ -1032,6 +1070,70 @@ void ora_dot(int n, int len, const void *x, int incx, const void *y, int incy, v
         for (int i = t; i < g3; i += b3) mp_add(c, &s[t], &s[t], &blk[i]);
     }
     block_tree(c, s, b3);
+    store_mp(n, r, 0, &s[0]);
+    free(s);
+    free(blk);
+    free(part);
+}
+
+void ora_add_abs(int n, const void *x, const void *y, void *r, long count) {
+    const ora_ctx_t *c = ora_init(n);
+    for (long i = 0; i < count; i++) {
+        mpf_t a, b, out;
+        load_mp(n, x, i, &a);
+        load_mp(n, y, i, &b);
+        mp_add_abs(c, &out, &a, &b);
+        store_mp(n, r, i, &out);
+    }
+}
+
+static void block_tree_abs(const ora_ctx_t *c, mpf_t *s, int bsize) {
+    for (unsigned i = next_pow2((unsigned)bsize) >> 1; i >= 1; i >>= 1)
+        for (unsigned t = 0; t < i; t++)
+            if (t + i < (unsigned)bsize) mp_add_abs(c, &s[t], &s[t], &s[t + i]);
+}
+
+/* cuda::mp_dot<blocks, threads> (src/blas/v2/dot_v2.cuh) and the sum of squares
+ * of cuda::mp_norm2<blocks, threads> (src/blas/v2/norm2_v2.cuh:39-123, with
+ * mp_add_abs): the v1 two-pass order over AoS vectors with unit strides.
+ * sumsq: r[0] = sum |x_i x_i|, y unused. */
+void ora_reduce_v2(int n, int sumsq, int len, const void *x, const void *y, void *r, int blocks, int threads) {
+    const ora_ctx_t *c = ora_init(n);
+    const long K = (long)blocks * threads;
+    mpf_t *part = (mpf_t *)malloc(sizeof(mpf_t) * K);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (long p = 0; p < K; p++) {
+        mpf_t acc, a, b, prod;
+        mp_zero(&acc);
+        for (long i = p; i < len; i += K) {
+            load_mp(n, x, i, &a);
+            if (sumsq) {
+                mp_mul(c, &prod, &a, &a);
+                mp_add_abs(c, &acc, &acc, &prod);
+            } else {
+                load_mp(n, y, i, &b);
+                mp_mul(c, &prod, &a, &b);
+                mp_add(c, &acc, &acc, &prod);
+            }
+        }
+        part[p] = acc;
+    }
+    mpf_t *blk = (mpf_t *)malloc(sizeof(mpf_t) * blocks);
+    for (int b = 0; b < blocks; b++) {
+        if (sumsq) block_tree_abs(c, &part[(long)b * threads], threads);
+        else block_tree(c, &part[(long)b * threads], threads);
+        blk[b] = part[(long)b * threads];
+    }
+    mpf_t *s = (mpf_t *)malloc(sizeof(mpf_t) * threads);
+    for (int t = 0; t < threads; t++) {
+        mp_zero(&s[t]);
+        for (int i = t; i < blocks; i += threads) {
+            if (sumsq) mp_add_abs(c, &s[t], &s[t], &blk[i]);
+            else mp_add(c, &s[t], &s[t], &blk[i]);
+        }
+    }
+    if (sumsq) block_tree_abs(c, s, threads);
+    else block_tree(c, s, threads);
     store_mp(n, r, 0, &s[0]);
     free(s);
     free(blk);

@@ -67,6 +67,8 @@ void ora_eval(int n, const int *digits, ora_er_t *low, ora_er_t *upp, long count
 void ora_scale2pow(int n, const int *digits, const unsigned *D, int *out, long count);
 
 /* BLAS in the reference kernels' summation order. */
+void ora_add_abs(int n, const void *x, const void *y, void *r, long count);
+void ora_reduce_v2(int n, int sumsq, int len, const void *x, const void *y, void *r, int blocks, int threads);
 void ora_dot(int n, int len, const void *x, int incx, const void *y, int incy, void *r, int g3, int b3);
 void ora_gemv(int n, int trans, int m, int cols, const void *alpha, const void *A, int lda, const void *x,
               int incx, const void *beta, void *y, int incy, int b3);

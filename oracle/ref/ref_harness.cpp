@@ -22,6 +22,8 @@
 #include "arith/muld.cuh"
 #include "arith/div.cuh"
 #include "arith/sqrt.cuh"
+#include "arith/addabs.cuh"
+#include "arith/sub.cuh"
 #include "mpvector.cuh"
 #include "mpmatrix.cuh"
 #include "mpreduct.cuh"
@@ -367,6 +369,122 @@ void ref_dsqrt(const mp_float_t *x, double *r, long count) {
         mp_float_t a = x[i];
         r[i] = ::mp_dsqrt(&a);
     }
+}
+
+/* cuda::mp_add_abs (src/arith/addabs.cuh:118-127), element by element */
+void ref_add_abs(const mp_float_t *x, const mp_float_t *y, mp_float_t *r, long count) {
+    for (long i = 0; i < count; i++) cuda::mp_add_abs(&r[i], x[i], y[i]);
+}
+
+/* mp_sumsq_kernel1/2 of cuda::mp_norm2<blocks, threads> (src/blas/v2/norm2_v2.cuh:39-112)
+ * and mp_dot_kernel1/2 of cuda::mp_dot<blocks, threads> (src/blas/v2/dot_v2.cuh),
+ * transcribed with one block's shared array at a time: the kernels keep their
+ * partial sums in static __shared__ arrays, which the coroutine launcher cannot
+ * share.  The arithmetic is the reference's device functions. */
+static void v2_reduce(bool sumsq, int n, const mp_float_t *x, const mp_float_t *y, mp_float_t *r, int blocks,
+                      int threads) {
+    const unsigned POW = nextPow2(threads);
+    std::vector<mp_float_t> parts(blocks), sdata(threads);
+    mp_float_t prod;
+    auto add = [&](mp_float_t *d, const mp_float_t &a, const mp_float_t &b) {
+        if (sumsq) cuda::mp_add_abs(d, a, b);
+        else cuda::mp_add(d, a, b);
+    };
+    auto tree = [&](int bsize) {
+        for (unsigned i = POW >> 1; i >= 1; i >>= 1)
+            for (unsigned tid = 0; tid < i; tid++)
+                if (tid + i < (unsigned)bsize) add(&sdata[tid], sdata[tid], sdata[tid + i]);
+    };
+    const unsigned k = (unsigned)blocks * threads;
+    for (int bid = 0; bid < blocks; bid++) {
+        for (int tid = 0; tid < threads; tid++) {
+            sdata[tid] = cuda::MP_ZERO;
+            for (unsigned i = bid * threads + tid; i < (unsigned)n; i += k) {
+                cuda::mp_mul(&prod, x[i], sumsq ? x[i] : y[i]);
+                add(&sdata[tid], sdata[tid], prod);
+            }
+        }
+        tree(threads);
+        parts[bid] = sdata[0];
+    }
+    for (int tid = 0; tid < threads; tid++) {
+        sdata[tid] = cuda::MP_ZERO;
+        for (unsigned i = tid; i < (unsigned)blocks; i += threads) add(&sdata[tid], sdata[tid], parts[i]);
+    }
+    tree(threads);
+    r[0] = sdata[0];
+}
+
+void ref_reduce_v2(int sumsq, int n, const mp_float_t *x, const mp_float_t *y, mp_float_t *r, int blocks, int threads) {
+    v2_reduce(sumsq != 0, n, x, y, r, blocks, threads);
+}
+
+/* mp_cg_csr / mp_pcg_csr (src/sparse/solver/cg_csr.cuh, pcg_csr.cuh) with the
+ * launch sequence transcribed: mp_spmv_csr runs as written; the v2 vector
+ * kernels (diff, axpy, maxpy, prod_d: one device function per element) and the
+ * reductions are transcribed as above; mp_div and mp_dsqrt are the reference's
+ * host MPFR functions.  M == nullptr: plain CG. */
+int ref_cg_csr(int n, const int *irp, const int *ja, const double *as, const mp_float_t *b, double tol, int maxit,
+               const double *M, mp_float_t *x, double *resvec, int cap, int threads, int blocks_reduce) {
+    std::vector<mp_float_t> r(n), p(n), q(n), z(n);
+    mp_float_t rho = cuda::MP_ZERO, rhop, alpha, beta, pq, nrm;
+    csr_t A;
+    A.irp = (int *)irp; A.ja = (int *)ja; A.as = (double *)as;
+    auto spmv = [&](mp_float_t *in, mp_float_t *out) {
+        emu::launch(dim3(n / threads + 1), dim3(threads), [&] {
+            if (threads == 32) cuda::mp_spmv_csr<32>(n, A, in, out);
+            else cuda::mp_spmv_csr<64>(n, A, in, out);
+        }, false);
+    };
+    auto norm2 = [&](const mp_float_t *v) {
+        v2_reduce(true, n, v, v, &nrm, blocks_reduce, threads);
+        return ::mp_dsqrt(&nrm);
+    };
+    spmv(x, r.data());
+    for (int i = 0; i < n; i++) cuda::mp_sub(&r[i], b[i], r[i]);
+    const double norm0 = norm2(r.data());
+    const double eps = norm0 * tol;
+    double normk = norm0;
+    int nres = 0, k = 0;
+    if (nres < cap) resvec[nres] = normk / norm0;
+    nres++;
+    mp_float_t *zz = M ? z.data() : r.data();
+    while (normk > eps && k < maxit) {
+        if (M)
+            for (int i = 0; i < n; i++) cuda::mp_mul_d(&z[i], r[i], M[i]);
+        rhop = rho;
+        v2_reduce(false, n, r.data(), zz, &rho, blocks_reduce, threads);
+        if (k == 0) {
+            for (int i = 0; i < n; i++) p[i] = zz[i];
+        } else {
+            ::mp_div(&beta, &rho, &rhop);
+            for (int i = 0; i < n; i++) {
+                mp_float_t ax;
+                cuda::mp_mul(&ax, beta, p[i]);
+                cuda::mp_add(&p[i], ax, zz[i]);
+            }
+        }
+        spmv(p.data(), q.data());
+        v2_reduce(false, n, p.data(), q.data(), &pq, blocks_reduce, threads);
+        ::mp_div(&alpha, &rho, &pq);
+        for (int i = 0; i < n; i++) {
+            mp_float_t ax;
+            cuda::mp_mul(&ax, alpha, p[i]);
+            cuda::mp_add(&x[i], ax, x[i]);
+        }
+        mp_float_t malpha = alpha;
+        malpha.sign = malpha.sign ^ 1;
+        for (int i = 0; i < n; i++) {
+            mp_float_t ax;
+            cuda::mp_mul(&ax, malpha, q[i]);
+            cuda::mp_add(&r[i], ax, r[i]);
+        }
+        normk = norm2(r.data());
+        if (nres < cap) resvec[nres] = normk / norm0;
+        nres++;
+        k++;
+    }
+    return k;
 }
 
 /* The Matrix Market reader, src/sparse/utils/mtx_reader.cuh:52-101, :249-253,

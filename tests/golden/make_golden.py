@@ -9,7 +9,9 @@ fesetround().  This script feeds it seeded inputs and stores inputs and outputs
 (mp_float_t records, bit for bit).  The reference checkout is needed only here;
 the committed .npz files are what the tests read.
 
-    bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/ref/build_ref.sh && python tests/golden/make_golden.py [v2] [cg]
+
+(with group names, only those files are regenerated)
 """
 import pathlib
 import sys
@@ -116,10 +118,68 @@ def spmv_case(n, seed, m, kmax):
     return out
 
 
+def spd_csr(rng, m, per_row):
+    """A symmetric, strictly diagonally dominant (so positive definite) sparse
+    matrix in CSR: random off-diagonal N(0,1) entries mirrored, diagonal = sum
+    of |row| + 1."""
+    rows = {i: {} for i in range(m)}
+    for i in range(m):
+        for j in rng.choice(m, size=per_row, replace=False):
+            if j != i:
+                v = float(rng.standard_normal())
+                rows[i][int(j)] = v
+                rows[int(j)][i] = v
+    irp, ja, vals = [0], [], []
+    for i in range(m):
+        rows[i][i] = sum(abs(v) for v in rows[i].values()) + 1.0
+        for j in sorted(rows[i]):
+            ja.append(j)
+            vals.append(rows[i][j])
+        irp.append(len(ja))
+    return np.array(irp, np.int32), np.array(ja, np.int32), np.array(vals)
+
+
+def cg_case(n, seed, m):
+    """mp_cg_csr<32, 256> and mp_pcg_csr<64, 256> (Jacobi) on an SPD matrix."""
+    R = ffi.reference(n)
+    rng = np.random.default_rng(seed)
+    irp, ja, vals = spd_csr(rng, m, 3)
+    b = R.set_d(helpers.doubles(rng, m, -4, 4))
+    x0 = R.set_d(np.zeros(m))
+    diag = np.array([vals[irp[i] + list(ja[irp[i]:irp[i + 1]]).index(i)] for i in range(m)])
+    M = 1.0 / diag
+    out = dict(irp=irp, ja=ja, vals=vals, b=b, x0=x0, M=M)
+    for tag, kw in (("cg", dict(threads=32, blocks=256)), ("pcg", dict(M=M, threads=64, blocks=256))):
+        k, x, res = ffi.ref_cg(n, irp, ja, vals, b, 1e-30, 40, x0, **kw)
+        out.update({tag + "_x": x, tag + "_res": res, tag + "_iters": np.array([k])})
+    return out
+
+
+def v2_case(n, seed):
+    """mp_add_abs and the v2 dot / sum of squares."""
+    R = ffi.reference(n)
+    rng = np.random.default_rng(seed)
+    x = R.set_d(helpers.doubles(rng, 3000, -30, 30))
+    y = R.set_d(helpers.doubles(rng, 3000, -30, 30))
+    out = dict(x=x, y=y, add_abs=ffi.ref_add_abs(n, x, y))
+    for blocks, threads in ((256, 32), (256, 64), (7, 33)):
+        out["dot_%d_%d" % (blocks, threads)] = ffi.ref_reduce_v2(n, False, x, y, blocks, threads)
+        out["sumsq_%d_%d" % (blocks, threads)] = ffi.ref_reduce_v2(n, True, x, None, blocks, threads)
+    return out
+
+
 def main():
     if not ffi.ref_available(8):
         raise SystemExit("build the reference first: bash oracle/ref/build_ref.sh")
     base = helpers.SEED
+    only = set(sys.argv[1:])
+    if only:  # regenerate the named groups only: v2, cg
+        if "v2" in only:
+            for n in (8, 16):
+                np.savez_compressed(HERE / ("v2_%d.npz" % n), **v2_case(n, base + 200 + n))
+        if "cg" in only:
+            np.savez_compressed(HERE / "cg_8.npz", **cg_case(8, base + 210, 300))
+        return
     for n in (8, 16, 32):
         np.savez_compressed(HERE / ("elem_%d.npz" % n), **elem_case(n, base + 100 + n))
     np.savez_compressed(HERE / "dot_8.npz", **dot_case(8, base + 0, {
@@ -144,6 +204,9 @@ def main():
     np.savez_compressed(HERE / "gemm_32.npz", **gemm_case(32, base + 1, {"a": (24, 20, 28)}))
     np.savez_compressed(HERE / "gemm_8.npz", **gemm_case(8, base + 10, {"a": (17, 9, 33), "b": (5, 31, 1)}))
     np.savez_compressed(HERE / "spmv_8.npz", **spmv_case(8, base + 2, 600, 64))
+    for n in (8, 16):
+        np.savez_compressed(HERE / ("v2_%d.npz" % n), **v2_case(n, base + 200 + n))
+    np.savez_compressed(HERE / "cg_8.npz", **cg_case(8, base + 210, 300))
     print("golden vectors written to", HERE)
 
 

@@ -93,10 +93,25 @@ int main() {
     cuda::csr_init(csr, 10, 10);
     cuda::mp_spmv_csr<32>(10, csr, hx.data(), hy.data());
     cuda::mp_spmv_csrv<32, 4>(10, csr, hx.data(), hy.data());
+    /* the solver drivers (tests/sparse/solver/*) and their v2 kernels */
+    std::vector<double> resvec;
+    int it = mp_cg_csr<32, 256>(10, csr, hx.data(), 1e-12, 20, hy.data(), resvec);
+    std::vector<double> M(10, 1.0);
+    it += mp_pcg_csr<64, 256>(10, csr, hx.data(), 1e-12, 20, diag, M.data(), hy.data(), resvec);
+    cuda::mp_axpy(10, hx.data(), hx.data(), hy.data(), hy.data());
+    cuda::mp_dot<256, 32>(10, hx.data(), hy.data(), hx.data());
+    double nrm = cuda::mp_norm2<256, 32>(10, hx.data()) + mp_dsqrt(hx.data()) + cuda::mp_dsqrt(hx.data());
+    mp_div(hx.data(), hx.data(), hy.data());
     cuda::csr_clear(csr);
+    /* the Matrix Market reader */
+    int m, n2, lines, maxnzr, nzmd;
+    bool symm;
+    std::string dtype;
+    collect_mtx_stats("a.mtx", m, n2, lines, maxnzr, nzmd, symm, dtype);
+    build_csr("a.mtx", m, lines, lines, symm, csr);
     cuda::mp_array_device2host(hr.data(), r, 1);
     cuda::mp_array_clear(x);
-    return 0;
+    return it + (int)nrm;
 }
 """
 

@@ -167,3 +167,12 @@ def test_gemm_accuracy_within_bound(oracle):
                 + abs(be * val(g["a_C"][r + c * ldc]))
             u = Fraction(4, int(2 ** (helpers.LOG2M[32] / 2)))
             assert abs(got - exact) <= u * (k + 3) * scale * 2
+
+
+def test_add_abs_and_v2_reductions_match_reference_golden(oracle):
+    for n in (8, 16):
+        g = np.load(GOLD / ("v2_%d.npz" % n))
+        eq(oracle.add_abs(n, g["x"], g["y"]), g["add_abs"])
+        for blocks, threads in ((256, 32), (7, 33)):
+            eq(oracle.reduce_v2(n, True, g["x"], None, blocks, threads), g["sumsq_%d_%d" % (blocks, threads)])
+            eq(oracle.reduce_v2(n, False, g["x"], g["y"], blocks, threads), g["dot_%d_%d" % (blocks, threads)])
