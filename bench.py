@@ -53,10 +53,20 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of each kernel from the committed ncu summary, if any."""
+def traffic(kernel, algo_bytes=None):
+    """DRAM bytes (read + write) per launch of a kernel at the benchmark size, from
+    the committed ncu capture (profiles/ncu_traffic.json); for a capture of a
+    smaller case, scaled by algorithmic bytes when algo_bytes is given.  None if
+    the kernel was not captured."""
     p = ROOT / "profiles" / "ncu_traffic.json"
-    return json.loads(p.read_text()) if p.exists() else {}
+    if not p.exists():
+        return None
+    e = json.loads(p.read_text()).get("kernels", {}).get(kernel)
+    if not e:
+        return None
+    if algo_bytes is not None:
+        return e["bytes_per_launch"] / e["algorithmic_bytes"] * algo_bytes if e.get("algorithmic_bytes") else None
+    return e["bytes_per_launch"]
 
 
 class Clocks:
@@ -201,7 +211,7 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     per_launch = secs / steps
     achieved = w_int / per_launch
     roof = {"bound": "int", "achieved": achieved / 1e9, "peak": rates["mulmod"] / 1e9, "unit": "Gmulmod/s",
-            "frac": achieved / rates["mulmod"], "traffic": ncu_traffic().get("gemm_nn"),
+            "frac": achieved / rates["mulmod"], "traffic": traffic("gemm_nn"),
             "peak_source": "measured in this run: Barrett mulmod microkernel (probe.cu)",
             "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
 
@@ -245,7 +255,7 @@ def bench_dot(torch, mp, stream, steps, warmup, world, hbm):
     return {"workload": "mp_dot n=2^20, 8 moduli, order <512,128,8192,256,64>", "value": world * 2 * count / per,
             "unit": "MP ops/s", "ms_per_step": per * 1e3, "launches": 2 * steps,
             "roofline": {"bound": "hbm", "achieved": algo / per / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": algo / per / 1e9 / hbm, "traffic": ncu_traffic().get("dot_pass1")},
+                         "frac": algo / per / 1e9 / hbm, "traffic": traffic("dot_pass1")},
             "data": (mx, my)}
 
 
@@ -268,7 +278,8 @@ def bench_spmv(torch, mp, stream, steps, warmup, world, hbm):
                      "launches": steps,
                      "roofline": {"bound": "hbm", "achieved": algo / per / 1e9, "peak": hbm, "unit": "GB/s",
                                   "frac": algo / per / 1e9 / hbm,
-                                  "traffic": ncu_traffic().get("spmv_" + name)}}
+                                  "traffic": traffic({"csr": "spmv_csr_kernel",
+                                                      "csrv32": "spmv_csrv_kernel"}[name])}}
     return {"workload": "mp_spmv 2^20 rows, nnz=%d (power-law 1..1024), 8 moduli" % nnz, "results": out,
             "nnz": nnz}
 
@@ -401,7 +412,8 @@ def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
             "launches_plain": 2 * count, "bit_identical_first_wave": identical, "shape": info,
             "commit_s": commit_s,
             "roofline": {"bound": "hbm", "achieved": algo / t_batch / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": algo / t_batch / 1e9 / hbm, "traffic": None},
+                         "frac": algo / t_batch / 1e9 / hbm, "traffic": traffic("batch_kernel", algo),
+                         "traffic_scope": "all waves, scaled from one ncu capture by algorithmic bytes"},
             "data": "A, x, y: random draws from 2^23 seeded u*2^e values (e in [-32, 32]) converted on the GPU; "
                     "alpha, beta ~ U(-1, 1)"}
 

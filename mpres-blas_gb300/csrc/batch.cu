@@ -273,9 +273,11 @@ int shape_slot(int nmod) {
     return si * 64 + (dev >= 0 && dev < 64 ? dev : 0);
 }
 
+/* the kernel's shared-memory limit, raised once per process for each variant */
 template <int N, int MAXT> cudaError_t set_attr() {
-    return cudaFuncSetAttribute(batch_kernel<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                MAXT * (int)sizeof(mp_t<N>));
+    static cudaError_t done = cudaFuncSetAttribute(batch_kernel<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   MAXT * (int)sizeof(mp_t<N>));
+    return done;
 }
 
 template <int N, int MAXT> int occupancy(int threads) {
@@ -299,8 +301,18 @@ cudaError_t launch_n(const BatchHost &b, const BatchDev &d, int threads, int cta
     if (b.tasks.empty()) return cudaSuccess;
     BatchArgs a{d.gemv, d.dot, d.spmv, d.tasks, (int)b.tasks.size(), d.counters, d.buf1, d.parts};
     const size_t smem = (size_t)threads * sizeof(mp_t<N>);
-    if (threads <= 256) batch_kernel<N, 256><<<ctas, threads, smem, s>>>(a);
-    else batch_kernel<N, 1024><<<ctas, threads, smem, s>>>(a);
+    /* register budgets: 256-thread CTAs may use up to 255 registers a thread,
+     * 512 up to 128, 1024 up to 64 */
+    if (threads <= 256) {
+        if ((e = set_attr<N, 256>()) != cudaSuccess) return e;
+        batch_kernel<N, 256><<<ctas, threads, smem, s>>>(a);
+    } else if (threads <= 512) {
+        if ((e = set_attr<N, 512>()) != cudaSuccess) return e;
+        batch_kernel<N, 512><<<ctas, threads, smem, s>>>(a);
+    } else {
+        if ((e = set_attr<N, 1024>()) != cudaSuccess) return e;
+        batch_kernel<N, 1024><<<ctas, threads, smem, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
@@ -447,9 +459,13 @@ cudaError_t batch_launch(int nmod, const BatchHost &b, const BatchDev &d, int th
 }
 
 int batch_ctas_per_sm(int nmod, int threads) {
-    if (nmod == 8) return threads <= 256 ? occupancy<8, 256>(threads) : occupancy<8, 1024>(threads);
-    if (nmod == 16) return threads <= 256 ? occupancy<16, 256>(threads) : occupancy<16, 1024>(threads);
-    if (nmod == 32) return threads <= 256 ? occupancy<32, 256>(threads) : occupancy<32, 1024>(threads);
+#define MPRES_OCC(NN)                                                                               \
+    return threads <= 256 ? occupancy<NN, 256>(threads)                                             \
+                          : (threads <= 512 ? occupancy<NN, 512>(threads) : occupancy<NN, 1024>(threads))
+    if (nmod == 8) MPRES_OCC(8);
+    if (nmod == 16) MPRES_OCC(16);
+    if (nmod == 32) MPRES_OCC(32);
+#undef MPRES_OCC
     return 0;
 }
 
@@ -709,6 +725,7 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
     b->threads = cand[best].first;
     b->ctas = cand[best].second * sms;
     if ((e = plan_and_upload(b, b->threads, cap)) != cudaSuccess) return status_cuda(e, "mpres_batch_commit (tables)");
+    batch_ctas_per_sm(b->nmod, b->threads); /* raises the shared-memory limit before any capture */
     if (flags & MPRES_BATCH_GRAPH) {
         cudaStream_t cs;
         if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)

@@ -55,14 +55,17 @@ def main(which, full):
         mp.gemm(32, k, k, k, al, A, k, B, k, be, C, k)
     if "batch" in which:
         count = 512 if full else 64
-        sizes = np.exp(rng.uniform(np.log(32), np.log(1024), (count, 2))).astype(int)
+        brng = np.random.default_rng(3)  # its own generator: the same batch whatever ran before
+        sizes = np.exp(brng.uniform(np.log(32), np.log(1024), (count, 2))).astype(int)
+        algo = int(np.sum((sizes[:, 0] * sizes[:, 1] + sizes[:, 1] + 2 * sizes[:, 0]) * 104))
+        print("batch of %d GEMVs: %d algorithmic bytes" % (count, algo))
         a = mp.DeviceArray.from_host(16, mp.set_d(16, np.array([0.7])))
         b = mp.Batch(16)
         keep = []
         for m, n in sizes:
-            A = mp.DeviceArray.from_host(16, mp.set_d(16, rng.uniform(-1, 1, m * n)))
-            x = mp.DeviceArray.from_host(16, mp.set_d(16, rng.uniform(-1, 1, n)))
-            y = mp.DeviceArray.from_host(16, mp.set_d(16, rng.uniform(-1, 1, m)))
+            A = mp.DeviceArray.from_host(16, mp.set_d(16, brng.uniform(-1, 1, m * n)))
+            x = mp.DeviceArray.from_host(16, mp.set_d(16, brng.uniform(-1, 1, n)))
+            y = mp.DeviceArray.from_host(16, mp.set_d(16, brng.uniform(-1, 1, m)))
             keep.append((A, x, y))
             b.add_gemv(mp.NO_TRANS, int(m), int(n), a, A, int(m), x, a, y, b3=32)
         b.commit(0)
