@@ -87,40 +87,6 @@ template <int N> __device__ __forceinline__ void split_add(mp_t<N> &res, const m
     round_if_needed<N>(res);
 }
 
-/* p = A[ia] * B[ib] (mp_mul) with the digits multiplied as they arrive, four at
- * a time, so the operands' digits are never all held at once */
-template <int N>
-__device__ __forceinline__ void mul_from_soa(mp_t<N> &p, const SoA &A, int lenA, long long ia, const SoA &B, int lenB,
-                                             long long ib) {
-    const Tables<N> &t = T<N>();
-    const longlong2 *ea = reinterpret_cast<const longlong2 *>(A.eval);
-    const longlong2 *eb = reinterpret_cast<const longlong2 *>(B.eval);
-    er_t al, au, bl, bu;
-    {
-        const longlong2 x0 = __ldg(ea + ia), x1 = __ldg(ea + lenA + ia);
-        const longlong2 y0 = __ldg(eb + ib), y1 = __ldg(eb + lenB + ib);
-        al.frac = __longlong_as_double(x0.x); al.exp = x0.y;
-        au.frac = __longlong_as_double(x1.x); au.exp = x1.y;
-        bl.frac = __longlong_as_double(y0.x); bl.exp = y0.y;
-        bu.frac = __longlong_as_double(y1.x); bu.exp = y1.y;
-    }
-    p.exp = __ldg(A.exp + ia) + __ldg(B.exp + ib);
-    p.sign = __ldg(A.sign + ia) ^ __ldg(B.sign + ib);
-    p.ev[0] = er_md<false>(al, bl, t.unit_upp, t.unit_upp_recip);
-    p.ev[1] = er_md<true>(au, bu, t.unit_low, t.unit_low_recip);
-    const int4 *da = reinterpret_cast<const int4 *>(A.digits + (size_t)ia * N);
-    const int4 *db = reinterpret_cast<const int4 *>(B.digits + (size_t)ib * N);
-#pragma unroll
-    for (int q = 0; q < N / 4; q++) {
-        const int4 x = __ldg(da + q), y = __ldg(db + q);
-        p.d[4 * q + 0] = mulmod_i<N>(x.x, y.x, 4 * q + 0);
-        p.d[4 * q + 1] = mulmod_i<N>(x.y, y.y, 4 * q + 1);
-        p.d[4 * q + 2] = mulmod_i<N>(x.z, y.z, 4 * q + 2);
-        p.d[4 * q + 3] = mulmod_i<N>(x.w, y.w, 4 * q + 3);
-    }
-    round_if_needed<N>(p);
-}
-
 template <int N, int BX, int BY>
 __global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B, int ldb,
                                                   SoA beta, int *cd, int *cs, int *ce, er_t *cv, const int *clen,
@@ -132,8 +98,10 @@ __global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha
     mp_t<N> sum;
     set_zero<N>(sum);
     for (int i = 0; i < k; i++) {
-        mp_t<N> p, s;
-        mul_from_soa<N>(p, A, lenA, (long long)lda * i + row, B, lenB, (long long)col * ldb + i);
+        mp_t<N> a, b, p, s;
+        load_soa<N>(a, A.digits, A.sign, A.exp, A.eval, lenA, (long long)lda * i + row);
+        load_soa<N>(b, B.digits, B.sign, B.exp, B.eval, lenB, (long long)col * ldb + i);
+        mp_mul<N>(p, a, b);
         mp_add<N>(s, sum, p);
         sum = s;
     }

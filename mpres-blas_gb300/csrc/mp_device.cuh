@@ -212,13 +212,16 @@ __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &
  * LEN real leaves (missing leaves read 0); leaf(i) is evaluated on demand. */
 template <int SPAN, int LEN, bool UP, class F>
 __device__ __forceinline__ double psum_node(const F &leaf, int base) {
+    /* The leaves are directed-rounding products of non-negative residues and
+     * positive reciprocals, so every node is +0 or positive; adding the +0 of
+     * a missing subtree is then exact in either direction and is skipped. */
     if constexpr (SPAN == 2) {
-        return dadd<UP>(leaf(base), LEN > 1 ? leaf(base + 1) : 0.0);
+        if constexpr (LEN > 1) return dadd<UP>(leaf(base), leaf(base + 1));
+        else return leaf(base);
     } else {
         double s1 = psum_node<SPAN / 2, LEN, UP>(leaf, base);
-        double s2 = 0.0;
-        if constexpr (LEN > SPAN / 2) s2 = psum_node<SPAN / 2, LEN - SPAN / 2, UP>(leaf, base + SPAN / 2);
-        return dadd<UP>(s1, s2);
+        if constexpr (LEN > SPAN / 2) return dadd<UP>(s1, psum_node<SPAN / 2, LEN - SPAN / 2, UP>(leaf, base + SPAN / 2));
+        else return s1;
     }
 }
 __host__ __device__ constexpr int psum_span(int len) {
