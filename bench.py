@@ -137,9 +137,16 @@ def max_over_ranks(value, world):
         return value
     import torch
     import torch.distributed as td
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cpu" if td.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     td.all_reduce(t, op=td.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(work_per_rank, secs, world):
+    """Whole-job throughput of `world` independent replicas that each did
+    work_per_rank units: all ranks' work over the slowest rank's time."""
+    return world * work_per_rank / max_over_ranks(secs, world)
 
 
 def barrier(world):

@@ -73,7 +73,8 @@ enum mpres_status {
     MPRES_ERR_INVALID_VALUE = 1, /* unsupported moduli set or argument */
     MPRES_ERR_NOT_INITIALIZED = 2,
     MPRES_ERR_CUDA = 3,          /* a CUDA runtime call or a kernel launch failed */
-    MPRES_ERR_NOT_SUPPORTED = 4  /* e.g. a transposed mp_gemm (the reference prints and returns) */
+    MPRES_ERR_NOT_SUPPORTED = 4, /* e.g. a transposed mp_gemm (the reference prints and returns) */
+    MPRES_ERR_CANCELLED = 5      /* a serving request withdrawn before it ran (mpres_gb300_server.h) */
 };
 
 /* mblas_trans_type values of src/blas/mblas_enum.cuh:25-29 */

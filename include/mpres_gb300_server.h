@@ -52,10 +52,15 @@ int mpres_server_submit_spmv_csr(mpres_server_t *server, int m, int ncols, long 
                                  const void *x, void *y, long long *id);
 
 /* blocks until request id is done (timeout_s < 0: no limit); MPRES_ERR_CUDA if
- * the loop met a CUDA error, MPRES_ERR_NOT_SUPPORTED on timeout */
+ * the loop met a CUDA error or the request could never fit the budget,
+ * MPRES_ERR_CANCELLED if it was cancelled, MPRES_ERR_NOT_SUPPORTED on timeout */
 int mpres_server_wait(mpres_server_t *server, long long id, double timeout_s);
 /* blocks until every request submitted so far is done */
 int mpres_server_drain(mpres_server_t *server);
+/* withdraws request id if it is still waiting for admission: it completes at
+ * once, its outputs untouched, and waiting for it returns MPRES_ERR_CANCELLED.
+ * MPRES_ERR_NOT_SUPPORTED if it was already launched or done. */
+int mpres_server_cancel(mpres_server_t *server, long long id);
 
 /* Per-request times in seconds since the server was created, for requests
  * [first, first + count): out[3*i] = submitted, out[3*i+1] = launched,

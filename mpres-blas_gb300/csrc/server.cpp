@@ -135,7 +135,8 @@ struct mpres_server {
     std::condition_variable cv_work, cv_done;
     std::deque<Req> pending;
     std::vector<Times> times;
-    std::vector<char> failed; /* per request: 1 if the loop could not run it */
+    std::vector<char> failed; /* per request: 1 if the loop could not run it, 2 if cancelled */
+    long long cancelled = 0;
     size_t inflight = 0, peak = 0;
     int busy = 0, max_busy = 0, errors = 0;
     long long done_count = 0, batches = 0, batched = 0;
@@ -519,8 +520,27 @@ int mpres_server_wait(mpres_server_t *s, long long id, double timeout_s) {
     if (timeout_s < 0) s->cv_done.wait(lk, ready);
     else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), ready))
         return status_fail(MPRES_ERR_NOT_SUPPORTED, "mpres_server_wait: request %lld not done in %.3f s", id, timeout_s);
+    if (s->failed[id] == 2) return status_fail(MPRES_ERR_CANCELLED, "mpres_server_wait: request %lld was cancelled", id);
     if (s->failed[id]) return status_fail(MPRES_ERR_CUDA, "mpres_server_wait: request %lld failed", id);
     return status_ok();
+}
+
+int mpres_server_cancel(mpres_server_t *s, long long id) {
+    if (!s) return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_server_cancel: null server");
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (id < 0 || id >= (long long)s->times.size())
+        return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_server_cancel: no request %lld", id);
+    for (auto it = s->pending.begin(); it != s->pending.end(); ++it) {
+        if (it->id != id) continue;
+        s->pending.erase(it);
+        s->times[id].done = now(s);
+        s->failed[id] = 2;
+        s->done_count++;
+        s->cancelled++;
+        s->cv_done.notify_all();
+        return status_ok();
+    }
+    return status_fail(MPRES_ERR_NOT_SUPPORTED, "mpres_server_cancel: request %lld already launched or done", id);
 }
 
 int mpres_server_drain(mpres_server_t *s) {
@@ -529,7 +549,7 @@ int mpres_server_drain(mpres_server_t *s) {
     const long long target = (long long)s->times.size();
     s->cv_done.wait(lk, [&] { return s->done_count >= target; });
     for (long long i = 0; i < target; i++)
-        if (s->failed[i]) return status_fail(MPRES_ERR_CUDA, "mpres_server_drain: request %lld failed", i);
+        if (s->failed[i] == 1) return status_fail(MPRES_ERR_CUDA, "mpres_server_drain: request %lld failed", i);
     return status_ok();
 }
 

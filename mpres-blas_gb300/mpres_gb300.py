@@ -97,6 +97,7 @@ _SIGS = {
     "mpres_server_submit_spmv_csr": (I, [P, I, I, ctypes.c_longlong, P, P, P, P]),
     "mpres_server_wait": (I, [P, ctypes.c_longlong, ctypes.c_double]),
     "mpres_server_drain": (I, [P]),
+    "mpres_server_cancel": (I, [P, ctypes.c_longlong]),
     "mpres_server_times": (I, [P, ctypes.c_longlong, ctypes.c_longlong, P]),
     "mpres_server_stats": (I, [P, P]),
     "mpres_probe_mulmod": (I, [I, I, ctypes.c_longlong, P, P]),
@@ -573,6 +574,14 @@ class Server:
 
     def drain(self):
         check(lib().mpres_server_drain(self.h), "mpres_server_drain")
+
+    def cancel(self, rid):
+        """True if the request was withdrawn before it ran, False if it had started."""
+        rc = lib().mpres_server_cancel(self.h, rid)
+        if rc == 4:
+            return False
+        check(rc, "mpres_server_cancel")
+        return True
 
     def times(self, first, count):
         out = np.zeros(3 * count)

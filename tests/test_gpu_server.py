@@ -126,3 +126,33 @@ def test_budget_serialises_and_rejects(gpu):
         srv.destroy()  # reports the failed request
     for d in devs:
         assert len(ffi.mismatches(_result(gpu, d), want)) == 0
+
+
+def test_cancel_and_timeout(gpu):
+    """A request withdrawn while it waits for admission completes as cancelled
+    with its output untouched; waiting with a short limit on a request stuck
+    behind a long one times out; everything else still completes."""
+    rng = np.random.default_rng(helpers.SEED + 6)
+    big = dict(kind="gemv", m=1500, n=1500, A=gpu.set_d(N, helpers.doubles(rng, 1500 * 1500, -32, 32)),
+               x=gpu.set_d(N, helpers.doubles(rng, 1500, -32, 32)), y=gpu.set_d(N, helpers.doubles(rng, 1500, -32, 32)),
+               alpha=gpu.set_d(N, rng.uniform(-1, 1, 1)), beta=gpu.set_d(N, rng.uniform(-1, 1, 1)))
+    small = [dict(kind="dot", n=4096, x=gpu.set_d(N, helpers.doubles(rng, 4096, -16, 16)),
+                  y=gpu.set_d(N, helpers.doubles(rng, 4096, -16, 16)), r=gpu.set_d(N, np.zeros(1))) for _ in range(4)]
+    want = [_alone(gpu, r) for r in small]
+    srv = gpu.Server(N, budget_bytes=1 << 30, slots=1, max_batch_ops=1)  # one request at a time
+    bd = _device(gpu, big)
+    devs = [_device(gpu, r) for r in small]
+    ids = [_submit(srv, bd)] + [_submit(srv, d) for d in devs]
+    cancelled = srv.cancel(ids[-1])
+    with pytest.raises(gpu.MpresError):
+        srv.wait(ids[-2], 1e-4)  # still behind the GEMV
+    for i, d, w in zip(ids[1:], devs, want):
+        if i == ids[-1] and cancelled:
+            with pytest.raises(gpu.MpresError, match="cancelled"):
+                srv.wait(i, 60.0)
+            assert len(ffi.mismatches(_result(gpu, d), small[-1]["r"])) == 0  # untouched
+        else:
+            srv.wait(i, 60.0)
+            assert len(ffi.mismatches(_result(gpu, d), w)) == 0
+    srv.wait(ids[0], 60.0)
+    srv.destroy()
