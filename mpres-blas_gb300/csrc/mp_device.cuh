@@ -51,11 +51,49 @@ __device__ __forceinline__ double bdbl(uint64_t u) { return __longlong_as_double
 __device__ __forceinline__ bool dnz(double d) { return (dbits(d) << 1) != 0; }
 /* x < 0 for a non-NaN double */
 __device__ __forceinline__ bool dneg(double d) { return (dbits(d) >> 63) && dnz(d); }
+/* x > 0 for a non-NaN double */
+__device__ __forceinline__ bool dpos(double d) { return !(dbits(d) >> 63) && dnz(d); }
 /* x * f for f in {-1, 0, 1}: exactly the IEEE product, computed on bits */
 __device__ __forceinline__ double dscale_sign(double x, int f) {
     uint64_t u = dbits(x);
     if (f == 0) return bdbl(u & kSign);
     return f < 0 ? bdbl(u ^ kSign) : x;
+}
+
+/* Conversions between integers and doubles on the integer pipes.  On GB300 a
+ * conversion instruction (I2F.F64, F2I.F64) or a double comparison occupies the
+ * FP64 pipe like an arithmetic operation: one warp instruction per 64 cycles of
+ * each SM sub-partition, measured, with no overlap between independent ones.
+ * These bit forms give the same values exactly. */
+
+/* (double)v for 0 <= v < 2^31 (exact: v has at most 31 significant bits),
+ * assembled from two 32-bit words */
+__device__ __forceinline__ double u31_to_double(uint32_t v) {
+    const int lz = __clz(v | 1u);
+    const uint32_t f = v << (lz + 1); /* the fraction bits below the leading 1 */
+    const uint32_t hi = ((uint32_t)(1054 - lz) << 20) | (f >> 12);
+    return v ? __hiloint2double((int)hi, (int)(f << 20)) : 0.0;
+}
+/* (unsigned int)x, truncating, for +0 <= x < 2^32 */
+__device__ __forceinline__ uint32_t d_trunc_u32(double x) {
+    const uint64_t a = dbits(x);
+    const int e = (int)(a >> 52) - 1023;
+    const uint64_t m = (a & ((1ull << 52) - 1)) | (1ull << 52);
+    return e < 0 ? 0u : (uint32_t)(m >> (52 - e));
+}
+/* x - (double)(unsigned int)x with the subtraction rounded downward (UP =
+ * false) or upward, for +0 <= x < 2^32.  The difference is exact, so only a
+ * zero result depends on the direction: -0 downward, +0 upward. */
+template <bool UP> __device__ __forceinline__ double d_frac(double x) {
+    const uint64_t a = dbits(x);
+    const int e = (int)(a >> 52) - 1023;
+    const double zero = UP ? 0.0 : -0.0;
+    if (e < 0) return a ? x : zero;
+    const uint64_t f = a & ((1ull << (52 - e)) - 1); /* the bits below the binary point */
+    if (!f) return zero;
+    const int L = 64 - __clzll((long long)f);
+    const uint64_t m = (f << (53 - L)) & ((1ull << 52) - 1);
+    return bdbl(((uint64_t)(L + e + 970) << 52) | m); /* f * 2^(e-52): exponent L-1+e-52 */
 }
 
 template <bool UP> __device__ __forceinline__ double dadd(double a, double b) {
@@ -167,28 +205,28 @@ template <bool UP> __device__ __forceinline__ double div_by_const(double p, doub
     double q = __dmul_rn(p, zr);
     if (!UP) {
         /* largest q with q*z <= p */
-        if (__fma_rn(-q, z, p) < 0.0) {
+        if (dneg(__fma_rn(-q, z, p))) {
             q = next_down(q);
-            if (__fma_rn(-q, z, p) < 0.0) q = next_down(q);
+            if (dneg(__fma_rn(-q, z, p))) q = next_down(q);
         } else {
             double qn = next_up(q);
-            if (__fma_rn(-qn, z, p) >= 0.0) {
+            if (!dneg(__fma_rn(-qn, z, p))) {
                 q = qn;
                 qn = next_up(q);
-                if (__fma_rn(-qn, z, p) >= 0.0) q = qn;
+                if (!dneg(__fma_rn(-qn, z, p))) q = qn;
             }
         }
     } else {
         /* smallest q with q*z >= p */
-        if (__fma_rn(-q, z, p) > 0.0) {
+        if (dpos(__fma_rn(-q, z, p))) {
             q = next_up(q);
-            if (__fma_rn(-q, z, p) > 0.0) q = next_up(q);
+            if (dpos(__fma_rn(-q, z, p))) q = next_up(q);
         } else {
             double qn = next_down(q);
-            if (__fma_rn(-qn, z, p) <= 0.0) {
+            if (!dpos(__fma_rn(-qn, z, p))) {
                 q = qn;
                 qn = next_down(q);
-                if (__fma_rn(-qn, z, p) <= 0.0) q = qn;
+                if (!dpos(__fma_rn(-qn, z, p))) q = qn;
             }
         }
     }
@@ -330,7 +368,7 @@ template <int N>
 __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &upp) {
     const Tables<N> &t = T<N>();
     int K = 0;
-    for (int guard = 0; sumu < t.eval_acc && guard < 4096; guard++) {
+    for (int guard = 0; dbits(sumu) < dbits(t.eval_acc) && guard < 4096; guard++) {
         int k;
         if (!dnz(sumu)) {
             k = t.log2m; /* log2(0): the reference's index saturates past the table */
@@ -342,12 +380,12 @@ __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &u
         const int *row = t.pow2 + (size_t)k * N;
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
-        sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
-        sumu = __dsub_ru(sumu, (double)(unsigned int)sumu);
+        sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
+        sumu = d_frac<true>(sumu);
         K += k;
     }
-    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
-    suml = __dsub_rd(suml, (double)(unsigned int)suml);
+    double suml = psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); });
+    suml = d_frac<false>(suml);
     er_set_d(low, suml);
     er_set_d(upp, sumu);
     low.exp -= K;
@@ -388,16 +426,16 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
 #pragma unroll
     for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
 #if !MPRES_EVAL_FIXED_POINT
-    double suml = psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
-    double sumu = psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+    double suml = psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); });
+    double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
     if (!dnz(suml) && !dnz(sumu)) {
         low.frac = 0.0; low.exp = 0;
         upp.frac = 0.0; upp.exp = 0;
         return;
     }
-    suml = __dsub_rd(suml, (double)(unsigned int)suml);
-    sumu = __dsub_ru(sumu, (double)(unsigned int)sumu);
-    if (sumu >= t.eval_acc) {
+    suml = d_frac<false>(suml);
+    sumu = d_frac<true>(sumu);
+    if (dbits(sumu) >= dbits(t.eval_acc)) {
         er_set_d(low, suml);
         er_set_d(upp, sumu);
         return;
@@ -428,8 +466,8 @@ template <int N> __device__ __forceinline__ int rank_full(const int *x, const in
     const unsigned int whu = fx_whole(fx_fraction_sum<N, true>(s));
 #else
     const Tables<N> &t = T<N>();
-    const unsigned int whl = (unsigned int)psum<N, false>([&](int i) { return __dmul_rd((double)s[i], t.recip_rd[i]); });
-    const unsigned int whu = (unsigned int)psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+    const unsigned int whl = d_trunc_u32(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
+    const unsigned int whu = d_trunc_u32(psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); }));
 #endif
     if (whl == whu) return (int)whl;
     return (mrd<N>(x) == 0) ? (int)whu : (int)whl;
@@ -440,7 +478,7 @@ template <int N> __device__ __forceinline__ int rank_fast(const int *s) {
     return (int)fx_whole(fx_fraction_sum<N, true>(s));
 #else
     const Tables<N> &t = T<N>();
-    return (int)psum<N, true>([&](int i) { return __dmul_ru((double)s[i], t.recip_ru[i]); });
+    return (int)d_trunc_u32(psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); }));
 #endif
 }
 
@@ -666,14 +704,15 @@ template <int N> __device__ __forceinline__ void mp_mul(mp_t<N> &r, const mp_t<N
 template <int N> __device__ __forceinline__ void mp_mul_d(mp_t<N> &r, const mp_t<N> &x, double y) {
     const Tables<N> &t = T<N>();
     const uint64_t u = dbits(y);
-    const bool ynz = y != 0;
+    const bool ynz = dnz(y);
     const uint64_t significand = ynz ? ((u & ((1ull << 52) - 1)) | (1ull << 52)) : 0ull;
     const int yexp = (int)(((u >> 52) & 2047) - (ynz ? (uint64_t)(1023 + 52) : 0ull));
     r.exp = x.exp + yexp;
     r.sign = x.sign ^ (int)(u >> 63);
     r.ev[0].exp = x.ev[0].exp;
     r.ev[1].exp = x.ev[1].exp;
-    const double sd = (double)significand;
+    /* (double)significand: 2^52 <= significand < 2^53, or 0 */
+    const double sd = ynz ? bdbl((1075ull << 52) | (significand & ((1ull << 52) - 1))) : 0.0;
     r.ev[0].frac = __dmul_rd(x.ev[0].frac, sd);
     r.ev[1].frac = __dmul_ru(x.ev[1].frac, sd);
     er_adjust(r.ev[0]);
