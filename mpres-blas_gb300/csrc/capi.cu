@@ -117,6 +117,8 @@ void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, co
     t.eval_acc_fx[1] = h.eval_acc_fx[1];
     t.unit_upp_recip = h.unit_upp_recip;
     t.unit_low_recip = h.unit_low_recip;
+    t.unit_upp_inv = h.unit_upp_inv;
+    t.unit_low_inv = h.unit_low_inv;
 }
 
 template <int N>

@@ -79,6 +79,17 @@ bool mantissa_at(double v, int shift, uint64_t &M) {
     return true;
 }
 
+/* floor(2^116 / Z) for the 53-bit significand Z of a positive normal double,
+ * saturated at 2^64 - 1 (Z = 2^52); the device's integer er_md divides by Z
+ * with it */
+static uint64_t significand_inverse(double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, sizeof(u));
+    const uint64_t z = (u & ((1ull << 52) - 1)) | (1ull << 52);
+    const unsigned __int128 q = (((unsigned __int128)1) << 116) / z;
+    return q >> 64 ? ~0ull : (uint64_t)q;
+}
+
 /* the integer forms the fixed-point evaluation uses (every recip is R * 2^-83
  * with a 53-bit R; eval_acc as the 128-bit ceiling of eval_acc * 2^83); false
  * if a constant is outside that range */
@@ -102,6 +113,8 @@ bool compute_fixed_forms(HostTables &t) {
     if (!(t.unit_upp.frac > 0) || !(t.unit_low.frac > 0)) return false;
     t.unit_upp_recip = 1.0 / t.unit_upp.frac;
     t.unit_low_recip = 1.0 / t.unit_low.frac;
+    t.unit_upp_inv = significand_inverse(t.unit_upp.frac);
+    t.unit_low_inv = significand_inverse(t.unit_low.frac);
     return true;
 }
 

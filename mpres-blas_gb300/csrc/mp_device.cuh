@@ -158,28 +158,24 @@ __device__ __forceinline__ void er_set_d(er_t &r, double x) {
 __device__ __forceinline__ double scale2(double x, int n) {
     const uint64_t u = dbits(x);
     const int e = (int)((u >> 52) & 2047);
-    if (e != 0 && e != 2047 && e + n >= 1 && e + n <= 2046)
+    if (n == 0 || (e != 0 && e != 2047 && e + n >= 1 && e + n <= 2046))
         return bdbl(u + ((uint64_t)(int64_t)n << 52));
     return scalbn(x, n);
 }
 
-/* er_add_rd / er_add_ru, src/extrange.cuh:451-490 */
-template <bool UP> __device__ __forceinline__ er_t er_add(er_t x, er_t y) {
+/* er_add_rd / er_add_ru, src/extrange.cuh:451-490: the operand with the larger
+ * exponent keeps its fraction, the other is scaled to it, one directed addition.
+ * Written with selects rather than the reference's three branches: a branch
+ * costs a single warp about as much as several integer instructions. */
+template <bool UP> __device__ __forceinline__ er_t er_add(const er_t &x, const er_t &y) {
     const bool xnz = dnz(x.frac), ynz = dnz(y.frac);
-    if (!xnz) x.exp = 0;
-    if (!ynz) y.exp = 0;
-    const long long dexp = (xnz && ynz) ? x.exp - y.exp : 0;
+    const long long xe = xnz ? x.exp : 0, ye = ynz ? y.exp : 0;
+    const long long dexp = (xnz && ynz) ? xe - ye : 0;
+    const bool swap = dexp < 0;
+    const double big = swap ? y.frac : x.frac, small = swap ? x.frac : y.frac;
     er_t r;
-    if (dexp > 0) {
-        r.exp = x.exp;
-        r.frac = dadd<UP>(x.frac, scale2(y.frac, (int)-dexp));
-    } else if (dexp < 0) {
-        r.exp = y.exp;
-        r.frac = dadd<UP>(y.frac, scale2(x.frac, (int)dexp));
-    } else {
-        r.exp = (x.exp == 0) ? y.exp : x.exp;
-        r.frac = dadd<UP>(x.frac, y.frac);
-    }
+    r.exp = dexp != 0 ? (swap ? ye : xe) : (xe == 0 ? ye : xe);
+    r.frac = dadd<UP>(big, scale2(small, (int)(swap ? dexp : -dexp)));
     er_adjust(r);
     return r;
 }
@@ -233,11 +229,67 @@ template <bool UP> __device__ __forceinline__ double div_by_const(double p, doub
     return q;
 }
 
-/* er_md_rd / er_md_ru (x*y/z), src/extrange.cuh:627-644; z is RNS_EVAL_UNIT's
- * upper (RD) or lower (RU) bound and zr the nearest double to its reciprocal */
+/* er_md_rd / er_md_ru (x*y/z), src/extrange.cuh:627-644: the fractions'
+ * product rounded in the direction, divided by z.frac rounded in the direction,
+ * then er_adjust.  z is RNS_EVAL_UNIT's upper (RD) or lower (RU) bound, zr the
+ * nearest double to 1/z.frac and zinv = floor(2^116 / Z), Z the 53-bit
+ * significand of z.frac.
+ *
+ * For fractions with |frac| in [1, 2) (as er_adjust leaves them) and for zeros,
+ * both roundings run on the integer pipes.  The 106-bit product P of the
+ * significands is cut to 53 bits p (plus one unit when rounding the magnitude
+ * up and a dropped bit is set).  With k = 52 if p >= Z, else 53, the quotient
+ * Q = floor(p * 2^k / Z) lies in [2^52, 2^53); q0 = floor(p * zinv / 2^(116-k))
+ * is Q or Q - 1 (the error of zinv contributes less than 2^-10), the remainder
+ * p * 2^k - q0 * Z < 2Z fits 64 bits, and one comparison with Z corrects q0 and
+ * yields the remainder that decides the directed rounding.  Other operands use
+ * the FP64 intrinsics. */
 template <bool UP>
-__device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z, double zr) {
+__device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z, double zr, uint64_t zinv) {
+    constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
+    const uint64_t bx = dbits(x.frac), by = dbits(y.frac);
+    const uint32_t ex = (uint32_t)(bx >> 52) & 2047u, ey = (uint32_t)(by >> 52) & 2047u;
+    const uint64_t sgn = (bx ^ by) & kSign;
     er_t r;
+    if (ex == 1023u && ey == 1023u) {
+        const bool up = UP != (sgn != 0); /* round the magnitude up */
+        const uint64_t mx = (bx & kMant) | kHidden, my = (by & kMant) | kHidden;
+        const uint64_t hi = __umul64hi(mx, my), lo = mx * my; /* P in [2^104, 2^106) */
+        const int sh = (hi >> 41) ? 53 : 52;
+        uint64_t p = (hi << (64 - sh)) | (lo >> sh);
+        p += (up && (lo & ((1ull << sh) - 1))) ? 1u : 0u;
+        int e = sh; /* the product is p * 2^(e - 104) */
+        if (p >> 53) {
+            p >>= 1;
+            e++;
+        }
+        const uint64_t bz = dbits(z.frac);
+        const uint64_t mz = (bz & kMant) | kHidden;
+        const int ez = (int)((bz >> 52) & 2047) - 1023;
+        const bool k52 = p >= mz;
+        const uint64_t thi = __umul64hi(p, zinv), tlo = p * zinv;
+        uint64_t q = k52 ? thi : ((thi << 1) | (tlo >> 63));
+        uint64_t rem = (k52 ? (p << 52) : (p << 53)) - q * mz;
+        if (rem >= mz) {
+            q++;
+            rem -= mz;
+        }
+        q += (up && rem) ? 1u : 0u;
+        int E = e - 52 - ez - (k52 ? 52 : 53); /* the quotient is q * 2^E */
+        if (q >> 53) {
+            q >>= 1;
+            E++;
+        }
+        r.exp = x.exp + y.exp - z.exp + (long long)(E + 52);
+        r.frac = bdbl(sgn | kBiasExpMask | (q & kMant));
+        return r;
+    }
+    if (((bx << 1) == 0 && ey != 2047u) || ((by << 1) == 0 && ex != 2047u)) {
+        /* a zero factor: a signed zero, which er_adjust leaves with exponent 0 */
+        r.exp = 0;
+        r.frac = bdbl(sgn);
+        return r;
+    }
     r.exp = x.exp + y.exp - z.exp;
     r.frac = div_by_const<UP>(dmul<UP>(x.frac, y.frac), z.frac, zr);
     er_adjust(r);
@@ -693,8 +745,8 @@ template <int N> __device__ __forceinline__ void mp_mul(mp_t<N> &r, const mp_t<N
     const Tables<N> &t = T<N>();
     r.exp = x.exp + y.exp;
     r.sign = x.sign ^ y.sign;
-    r.ev[0] = er_md<false>(x.ev[0], y.ev[0], t.unit_upp, t.unit_upp_recip);
-    r.ev[1] = er_md<true>(x.ev[1], y.ev[1], t.unit_low, t.unit_low_recip);
+    r.ev[0] = er_md<false>(x.ev[0], y.ev[0], t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+    r.ev[1] = er_md<true>(x.ev[1], y.ev[1], t.unit_low, t.unit_low_recip, t.unit_low_inv);
 #pragma unroll
     for (int i = 0; i < N; i++) r.d[i] = mulmod_i<N>(x.d[i], y.d[i], i);
     round_if_needed<N>(r);

@@ -45,6 +45,8 @@ struct Tables {
     uint64_t eval_acc_fx[2];     /* ceil(RNS_EVAL_ACCURACY * 2^83) as {low, high} 64-bit words */
     double unit_upp_recip;       /* nearest double to 1 / RNS_EVAL_UNIT.upp.frac */
     double unit_low_recip;       /* nearest double to 1 / RNS_EVAL_UNIT.low.frac */
+    uint64_t unit_upp_inv;       /* floor(2^116 / Z), Z the 53-bit significand of RNS_EVAL_UNIT.upp.frac, at most 2^64-1 */
+    uint64_t unit_low_inv;       /* the same for RNS_EVAL_UNIT.low.frac */
     const int *ceil_log2_pow2;   /* device: ceil(log2(2^e)) by CUDA's log2, e = -1074..1023 */
     /* the host conversion (double -> mp_float_t) replayed on the device */
     double recip_rn[N];          /* 1.0 / m_i rounded to nearest, as the host computes it */
@@ -68,6 +70,7 @@ struct HostTables {
     int *pow2 = nullptr; /* host, (log2m + 1) * n */
     uint64_t recip_rd_m[32], recip_ru_m[32], eval_acc_fx[2]; /* the Tables<N> integer forms */
     double unit_upp_recip = 0, unit_low_recip = 0;
+    uint64_t unit_upp_inv = 0, unit_low_inv = 0;
 };
 
 /* Computes every table of the predefined set of n moduli (n in {8, 16, 32});
