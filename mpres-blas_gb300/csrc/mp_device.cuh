@@ -478,16 +478,20 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
 #pragma unroll
     for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
 #if !MPRES_EVAL_FIXED_POINT
-    double suml = psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); });
+    /* The lower sum is formed only when it is used: the refinement recomputes it
+     * from the refined residues.  Every leaf rounded down is at most the same
+     * leaf rounded up, so the lower sum is zero whenever the upper one is, and
+     * the reference's test that both are zero is the upper sum's. */
     double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
-    if (!dnz(suml) && !dnz(sumu)) {
+    if (!dnz(sumu)) {
         low.frac = 0.0; low.exp = 0;
         upp.frac = 0.0; upp.exp = 0;
         return;
     }
-    suml = d_frac<false>(suml);
     sumu = d_frac<true>(sumu);
     if (dbits(sumu) >= dbits(t.eval_acc)) {
+        const double suml =
+            d_frac<false>(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
         er_set_d(low, suml);
         er_set_d(upp, sumu);
         return;
