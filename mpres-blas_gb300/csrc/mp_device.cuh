@@ -682,14 +682,17 @@ template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N
     }
     r.sign = sign;
     r.exp = (ex == 0) ? ey : ex;
-    /* cuda::rns_axby_cd, src/modular.cuh:306-314: (2^gamma*x*fx + 2^theta*y*fy) mod m */
-    const int *pg = t.pow2 + (size_t)pow2_row_index<N>(gamma) * N;
-    const int *pt = t.pow2 + (size_t)pow2_row_index<N>(theta) * N;
+    /* cuda::rns_axby_cd, src/modular.cuh:306-314: (2^gamma*x*fx + 2^theta*y*fy) mod m.
+     * At most one of gamma, theta is nonzero, so one modular product per
+     * residue scales the operand that needs it (row 0 holds 2^0 = 1). */
+    const bool gx = gamma != 0;
+    const int *pw = t.pow2 + (size_t)pow2_row_index<N>(gx ? gamma : theta) * N;
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t m = (uint32_t)t.moduli[i];
-        uint32_t u = gamma ? mulmod((uint32_t)__ldg(pg + i), (uint32_t)x.d[i], m, t.mu[i]) : (uint32_t)x.d[i];
-        uint32_t v = theta ? mulmod((uint32_t)__ldg(pt + i), (uint32_t)y.d[i], m, t.mu[i]) : (uint32_t)y.d[i];
+        const uint32_t w = mulmod((uint32_t)__ldg(pw + i), (uint32_t)(gx ? x.d[i] : y.d[i]), m, t.mu[i]);
+        const uint32_t u = gx ? w : (uint32_t)x.d[i];
+        const uint32_t v = gx ? (uint32_t)y.d[i] : w;
         uint32_t a = fx > 0 ? u : (fx < 0 ? (u ? m - u : 0u) : 0u);
         uint32_t b = fy > 0 ? v : (fy < 0 ? (v ? m - v : 0u) : 0u);
         uint32_t s = reduce2(a + b, m);
