@@ -91,6 +91,10 @@ template <int N, int BX, int BY>
 __global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B, int ldb,
                                                   SoA beta, int *cd, int *cs, int *ce, er_t *cv, const int *clen,
                                                   int ldc) {
+    __shared__ int pow2s[pow2_cache_words<N>()];
+    pow2_stage<N>(pow2s, threadIdx.y * BX + threadIdx.x, BX * BY);
+    __syncthreads();
+    const uint32_t cache = (uint32_t)__cvta_generic_to_shared(pow2s);
     const int row = blockIdx.x * BX + threadIdx.x;
     const int col = blockIdx.y * BY + threadIdx.y;
     if (row >= m || col >= n) return;
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha
         load_soa<N>(a, A.digits, A.sign, A.exp, A.eval, lenA, (long long)lda * i + row);
         load_soa<N>(b, B.digits, B.sign, B.exp, B.eval, lenB, (long long)col * ldb + i);
         mp_mul<N>(p, a, b);
-        mp_add<N>(s, sum, p);
+        mp_add<N>(s, sum, p, cache);
         sum = s;
     }
     const int lenC = __ldg(clen);

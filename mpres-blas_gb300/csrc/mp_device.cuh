@@ -635,9 +635,31 @@ template <int N> __device__ __forceinline__ void set_zero(mp_t<N> &z) {
     z.ev[1].frac = 0.0; z.ev[1].exp = 0;
 }
 
+/* RNS_POW2 rows 0 .. kPow2Rows-1 staged in shared memory for the aligned
+ * additions of a kernel.  The lanes of a warp align by different shifts, so a
+ * load of RNS_POW2[shift][i] from the global table touches up to 32 cache lines
+ * per instruction; measured with the rows made uniform (a timing-only copy),
+ * those loads were a third of mp_gemm 1024^3.  The copy (pow2_stage, then a
+ * barrier) has a row stride of N+1 words, so lanes on different rows mostly
+ * read different banks; larger shifts read the global table. */
+constexpr int kPow2Rows = 256;
+template <int N> __host__ __device__ constexpr int pow2_cache_words() { return kPow2Rows * (N + 1); }
+template <int N> __device__ __forceinline__ void pow2_stage(int *cache, int tid, int nthreads) {
+    const Tables<N> &t = T<N>();
+    const int rows = t.log2m + 1 < kPow2Rows ? t.log2m + 1 : kPow2Rows;
+    for (int w = tid; w < rows * N; w += nthreads) cache[(w / N) * (N + 1) + w % N] = __ldg(t.pow2 + w);
+}
+__device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
+    uint32_t v;
+    asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
+    return v;
+}
+
 /* cuda::mp_add: mp_add_common (src/arith/add.cuh:126-188) and the rounding of
- * its overloads (:190-271). */
-template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y) {
+ * its overloads (:190-271).  cache: the shared-memory address of a pow2_stage
+ * copy, or 0 for the global table. */
+template <int N>
+__device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<N> &y, uint32_t cache = 0) {
     const Tables<N> &t = T<N>();
     int ex = x.exp, ey = y.exp, sx = x.sign, sy = y.sign;
     const int dexp = ex - ey;
@@ -686,11 +708,21 @@ template <int N> __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N
      * At most one of gamma, theta is nonzero, so one modular product per
      * residue scales the operand that needs it (row 0 holds 2^0 = 1). */
     const bool gx = gamma != 0;
-    const int *pw = t.pow2 + (size_t)pow2_row_index<N>(gx ? gamma : theta) * N;
+    const int row = pow2_row_index<N>(gx ? gamma : theta);
+    const int *pw = t.pow2 + (size_t)row * N;
+    const bool cached = cache != 0 && row < kPow2Rows;
+    const uint32_t srow = cache + (uint32_t)((cached ? row : 0) * (N + 1)) * 4u;
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t m = (uint32_t)t.moduli[i];
-        const uint32_t w = mulmod((uint32_t)__ldg(pw + i), (uint32_t)(gx ? x.d[i] : y.d[i]), m, t.mu[i]);
+        uint32_t pv;
+        if (cache != 0) {
+            pv = lds_u32(srow + 4u * i);
+            if (!cached) pv = (uint32_t)__ldg(pw + i);
+        } else {
+            pv = (uint32_t)__ldg(pw + i);
+        }
+        const uint32_t w = mulmod(pv, (uint32_t)(gx ? x.d[i] : y.d[i]), m, t.mu[i]);
         const uint32_t u = gx ? w : (uint32_t)x.d[i];
         const uint32_t v = gx ? (uint32_t)y.d[i] : w;
         uint32_t a = fx > 0 ? u : (fx < 0 ? (u ? m - u : 0u) : 0u);
