@@ -640,19 +640,19 @@ template <int N> __device__ __forceinline__ void set_zero(mp_t<N> &z) {
  * load of RNS_POW2[shift][i] from the global table touches up to 32 cache lines
  * per instruction; measured with the rows made uniform (a timing-only copy),
  * those loads were a third of mp_gemm 1024^3.  The copy (pow2_stage, then a
- * barrier) has a row stride of N+1 words, so lanes on different rows mostly
- * read different banks; larger shifts read the global table. */
+ * barrier) has a row stride of N+4 words and is read four words at a time; lanes
+ * on different rows mostly read different banks.  Larger shifts read the global
+ * table. */
 constexpr int kPow2Rows = 256;
-template <int N> __host__ __device__ constexpr int pow2_cache_words() { return kPow2Rows * (N + 1); }
+template <int N> __host__ __device__ constexpr int pow2_cache_words() { return kPow2Rows * (N + 4); }
 template <int N> __device__ __forceinline__ void pow2_stage(int *cache, int tid, int nthreads) {
     const Tables<N> &t = T<N>();
     const int rows = t.log2m + 1 < kPow2Rows ? t.log2m + 1 : kPow2Rows;
-    for (int w = tid; w < rows * N; w += nthreads) cache[(w / N) * (N + 1) + w % N] = __ldg(t.pow2 + w);
+    for (int w = tid; w < rows * N; w += nthreads) cache[(w / N) * (N + 4) + w % N] = __ldg(t.pow2 + w);
 }
-__device__ __forceinline__ uint32_t lds_u32(uint32_t addr) {
-    uint32_t v;
-    asm("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(addr));
-    return v;
+/* four consecutive words of shared memory at a 16-byte aligned address */
+__device__ __forceinline__ void lds_v4(uint32_t addr, uint32_t (&v)[4]) {
+    asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(addr));
 }
 
 /* cuda::mp_add: mp_add_common (src/arith/add.cuh:126-188) and the rounding of
@@ -711,18 +711,21 @@ __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<
     const int row = pow2_row_index<N>(gx ? gamma : theta);
     const int *pw = t.pow2 + (size_t)row * N;
     const bool cached = cache != 0 && row < kPow2Rows;
-    const uint32_t srow = cache + (uint32_t)((cached ? row : 0) * (N + 1)) * 4u;
+    const uint32_t srow = cache + (uint32_t)((cached ? row : 0) * (N + 4)) * 4u;
+    uint32_t pv[4];
 #pragma unroll
     for (int i = 0; i < N; i++) {
         const uint32_t m = (uint32_t)t.moduli[i];
-        uint32_t pv;
-        if (cache != 0) {
-            pv = lds_u32(srow + 4u * i);
-            if (!cached) pv = (uint32_t)__ldg(pw + i);
-        } else {
-            pv = (uint32_t)__ldg(pw + i);
+        if (i % 4 == 0) {
+            if (cache != 0) {
+                lds_v4(srow + 4u * i, pv);
+                if (!cached)
+                    for (int e = 0; e < 4; e++) pv[e] = (uint32_t)__ldg(pw + i + e);
+            } else {
+                for (int e = 0; e < 4; e++) pv[e] = (uint32_t)__ldg(pw + i + e);
+            }
         }
-        const uint32_t w = mulmod(pv, (uint32_t)(gx ? x.d[i] : y.d[i]), m, t.mu[i]);
+        const uint32_t w = mulmod(pv[i % 4], (uint32_t)(gx ? x.d[i] : y.d[i]), m, t.mu[i]);
         const uint32_t u = gx ? w : (uint32_t)x.d[i];
         const uint32_t v = gx ? (uint32_t)y.d[i] : w;
         uint32_t a = fx > 0 ? u : (fx < 0 ? (u ? m - u : 0u) : 0u);
