@@ -92,9 +92,7 @@ __global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha
                                                   SoA beta, int *cd, int *cs, int *ce, er_t *cv, const int *clen,
                                                   int ldc) {
     __shared__ __align__(16) int pow2s[pow2_cache_words<N>()];
-    pow2_stage<N>(pow2s, threadIdx.y * BX + threadIdx.x, BX * BY);
-    __syncthreads();
-    const uint32_t cache = (uint32_t)__cvta_generic_to_shared(pow2s);
+    const uint32_t cache = pow2_cache_setup<N>(pow2s);
     const int row = blockIdx.x * BX + threadIdx.x;
     const int col = blockIdx.y * BY + threadIdx.y;
     if (row >= m || col >= n) return;

@@ -650,6 +650,13 @@ template <int N> __device__ __forceinline__ void pow2_stage(int *cache, int tid,
     const int rows = t.log2m + 1 < kPow2Rows ? t.log2m + 1 : kPow2Rows;
     for (int w = tid; w < rows * N; w += nthreads) cache[(w / N) * (N + 4) + w % N] = __ldg(t.pow2 + w);
 }
+/* every thread of the block stages the copy, then a barrier; returns its
+ * shared-memory address for mp_add */
+template <int N> __device__ __forceinline__ uint32_t pow2_cache_setup(int *cache) {
+    pow2_stage<N>(cache, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+    __syncthreads();
+    return (uint32_t)__cvta_generic_to_shared(cache);
+}
 /* four consecutive words of shared memory at a 16-byte aligned address */
 __device__ __forceinline__ void lds_v4(uint32_t addr, uint32_t (&v)[4]) {
     asm("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]) : "r"(addr));
