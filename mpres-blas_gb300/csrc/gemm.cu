@@ -87,8 +87,11 @@ template <int N> __device__ __forceinline__ void split_add(mp_t<N> &res, const m
     round_if_needed<N>(res);
 }
 
+/* Three 128-thread blocks per SM (at most 168 registers a thread): measured
+ * faster than two (255 registers) despite the spills, 94.8 against 108.0 ms at
+ * 1024^3; four (128 registers) spill too much. */
 template <int N, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY) gemm_nn(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B, int ldb,
+__global__ void __launch_bounds__(BX *BY, 3) gemm_nn(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B, int ldb,
                                                   SoA beta, int *cd, int *cs, int *ce, er_t *cv, const int *clen,
                                                   int ldc) {
     __shared__ __align__(16) int pow2s[pow2_cache_words<N>()];
