@@ -201,12 +201,22 @@ def probe_rates(torch, mp, stream):
 
 
 def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
+    """C = alpha*A*B + beta*C, m = n = k = 1024, 32 moduli.  Every step starts
+    from the same C, as the reference's own benchmark re-uploads C before each
+    timed call (tests/blas/performance/test_gemm_performance.cu): C accumulated
+    over steps would grow its residue representation by the bits of beta each
+    time and make the later steps round in the epilogue.  The restore is a
+    device-to-device copy inside the timed region."""
     n, m = 32, 1024
     host = gemm_inputs(mp, n, m)
     d = {k: mp.DeviceArray.from_host(n, v) for k, v in host.items()}
+    c_work, c_init = mp.TensorArray(n, m * m), mp.TensorArray(n, m * m)
+    c_init.upload(host["C"])
 
     def step():
-        mp.gemm(n, m, m, m, d["alpha"], d["A"], m, d["B"], m, d["beta"], d["C"], m, stream=stream)
+        with torch.cuda.stream(stream):
+            c_work.copy_(c_init)
+        mp.gemm(n, m, m, m, d["alpha"], d["A"], m, d["B"], m, d["beta"], c_work, m, stream=stream)
 
     with Clocks(local) as clk:
         secs = time_steps(torch, stream, step, steps, warmup, world)
@@ -676,7 +686,8 @@ def main():
         "data": "synthetic (seeded u*2^e entries; the reference publishes no dataset)",
         "config": {"workload": "mp_gemm m=n=k=1024, 32 moduli (params.32_32bit), NN, column-major",
                    "global_batch": 1, "seq_len": None, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (3 x 176 MB)"},
+                   "l2": "inputs larger than L2 (3 x 176 MB)",
+                   "c_per_step": "C restored from its initial value by a device copy inside each timed step"},
         "roofline": g["roofline"], "hbm_peak_source": peak_src, "e2e": g["e2e"], "clocks": g["clocks"],
         "gpu_launches": g["launches"],
     }

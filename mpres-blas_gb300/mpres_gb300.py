@@ -362,6 +362,28 @@ class TensorArray:
         """Device conversion of a float64 CUDA tensor into elements [offset, offset + x.numel())."""
         array_set_d(self.nmod, self, offset, x, stream)
 
+    def upload(self, host):
+        """Elements from a host mp_float_t array (the inverse of download)."""
+        import torch
+        host = np.ascontiguousarray(host)
+        assert host.dtype.itemsize == 4 * self.nmod + 40 and len(host) == self.size
+        dev = self.digits.device
+        self.digits.copy_(torch.from_numpy(np.ascontiguousarray(host["digits"]).reshape(-1)).to(dev))
+        self.sign.copy_(torch.from_numpy(np.ascontiguousarray(host["sign"])).to(dev))
+        self.exp.copy_(torch.from_numpy(np.ascontiguousarray(host["exp"])).to(dev))
+        ev = np.empty((2 * self.size, 2), np.int64)
+        for h in (0, 1):
+            ev[h * self.size:(h + 1) * self.size, 0] = np.ascontiguousarray(host["eval"][:, h]["frac"]).view(np.int64)
+            ev[h * self.size:(h + 1) * self.size, 1] = host["eval"][:, h]["exp"]
+        self.eval.copy_(torch.from_numpy(ev).to(dev))
+
+    def copy_(self, src):
+        """Every element from another TensorArray of the same size (device copies
+        on the current stream)."""
+        assert src.nmod == self.nmod and src.size == self.size
+        for a, b in ((self.digits, src.digits), (self.sign, src.sign), (self.exp, src.exp), (self.eval, src.eval)):
+            a.copy_(b)
+
     def download(self):
         out = np.zeros(self.size, mp_dtype(self.nmod))
         out["digits"] = self.digits.view(-1, self.nmod).cpu().numpy()

@@ -156,6 +156,21 @@ def test_gemm_random_vs_oracle(gpu, oracle, n, m, cols, k):
     eq(r, oracle.gemm(n, m, cols, k, al, A, lda, B, ldb, be, C, ldc))
 
 
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_gemm_wide_exponents_vs_oracle(gpu, oracle, n):
+    """Entries u * 2^e with e in [-400, 400]: the aligned additions of the k
+    chain shift by more than the 256 rows of powers of two that the GEMM kernel
+    stages in shared memory, so both the staged and the global table are read."""
+    m, cols, k = 24, 16, 40
+    rng = np.random.default_rng(helpers.SEED + 7 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, -400, 400))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, -400, 400))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, -400, 400))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    r = run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m)
+    eq(r, oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m))
+
+
 def test_gemm_transposed_is_not_supported(gpu):
     rec = gpu.set_d(8, np.ones(4))
     d = gpu.DeviceArray.from_host(8, rec)

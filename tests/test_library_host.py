@@ -127,3 +127,19 @@ def test_cpp_dropin_header_compiles_and_links(library, tmp_path):
                         str(tmp_path / "driver"), str(lib), "-Wl,-rpath," + str(lib.parent)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("n", [8, 32])
+def test_tensor_array_upload_copy_download(library, oracle, n):
+    """TensorArray.upload / copy_ / download keep mp_float_t records bit for bit
+    (the GEMM benchmark restores C with them); torch tensors on the CPU."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(helpers.SEED + 11)
+    host = oracle.set_d(n, np.concatenate([helpers.doubles(rng, 37, -40, 40), [0.0, -0.0, 1.0]]))
+    a = library.TensorArray(n, len(host), device="cpu")
+    a.upload(host)
+    b = library.TensorArray(n, len(host), device="cpu")
+    b.copy_(a)
+    assert a.download().tobytes() == host.tobytes()
+    assert b.download().tobytes() == host.tobytes()
+    assert torch.equal(a.eval, b.eval)
