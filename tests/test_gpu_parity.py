@@ -50,6 +50,9 @@ def test_dot_golden(gpu, name, n):
     (8, 100003, (1, 1, 1, 64, 64)),
     (8, 50000, (1, 1, 1, 37, 200)),
     (8, 4000, (1, 1, 1, 2, 1024)),
+    (8, 20011, (1, 1, 1, 45, 37)),
+    (8, 5000, (1, 1, 1, 7, 3)),
+    (8, 3001, (1, 1, 1, 1, 1)),
     (16, 30000, (512, 128, 8192, 256, 64)),
     (32, 20000, (512, 128, 8192, 96, 32)),
 ])
@@ -59,6 +62,18 @@ def test_dot_random_vs_oracle(gpu, oracle, n, count, order):
     my = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
     r = run_dot(gpu, n, mx, my, count, order)
     eq(r, oracle.dot(n, mx, my, g3=order[3], b3=order[4]))
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_dot_wide_exponents_vs_oracle(gpu, oracle, n):
+    """Entries u * 2^e with e in [-300, 300]: alignments by hundreds of bits,
+    zeroed negligible operands and roundings by more than one scaling step."""
+    rng = np.random.default_rng(helpers.SEED + 21 + n)
+    count = 30011
+    mx = gpu.set_d(n, helpers.doubles(rng, count, -300, 300))
+    my = gpu.set_d(n, helpers.doubles(rng, count, -300, 300))
+    r = run_dot(gpu, n, mx, my, count, (512, 128, 8192, 64, 64))
+    eq(r, oracle.dot(n, mx, my, g3=64, b3=64))
 
 
 def test_dot_strides_and_reuse(gpu, oracle):
