@@ -109,6 +109,7 @@ void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, co
     t.ceil_log2_pow2 = dceil;
     t.host_ceil_log2 = dhost_log2;
     for (int i = 0; i < N; i++) t.recip_rn[i] = 1.0 / (double)h.moduli[i];
+    for (int i = 0; i < N; i++) t.pow2_32[i] = (uint32_t)((1ull << 32) % (unsigned long long)h.moduli[i]);
     for (int i = 0; i < N; i++) {
         t.recip_rd_m[i] = h.recip_rd_m[i];
         t.recip_ru_m[i] = h.recip_ru_m[i];
@@ -683,7 +684,12 @@ int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_a
         return fail(MPRES_ERR_NOT_SUPPORTED, "mpres_gemm: only non-transposed matrices are supported");
     if (!alpha || !A || !B || !beta || !C) return fail(MPRES_ERR_INVALID_VALUE, "mpres_gemm: null array");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, s);
+    Workspace ws;
+    if (workspace(s, gemm_workspace_bytes(nmod, m, n, k), ws) != MPRES_SUCCESS) {
+        ws = Workspace{}; /* no room for W(A), W(B): the step-by-step chain, no scratch */
+        cudaGetLastError(); /* the failed allocation is not this call's error */
+    }
+    cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemm");
 }
 

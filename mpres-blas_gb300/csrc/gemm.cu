@@ -13,6 +13,28 @@
  * All three stages are fused here into one kernel per output tile with the same
  * arithmetic, so the buffer matrix never leaves registers.  The k chain keeps
  * the reference's order (no split-k), so results are bit-identical.
+ *
+ * Residues of the k chain, carried lazily.  The moduli are odd, so 2 is
+ * invertible modulo each of them and every number X = (-1)^s * D * 2^e has the
+ * residue vector W = (-1)^s * D * 2^e mod m_i, for negative e too.  mp_add
+ * aligns its operands by multiplying the one with the larger exponent by
+ * 2^(difference) and adds them with their signs; in terms of W that is
+ * W(x + y) = nzx * W(x) + nzy * W(y), where nzx, nzy are mp_add's flags that
+ * drop an operand too small to matter -- whatever the exponents, and whatever
+ * sign the sum is given.  mp_mul gives W(a * b) = W(a) * W(b).  So as long as
+ * no rounding intervenes (a rounding rescales the residues by a power of two
+ * with a remainder), the chain's residues are the plain modular dot product
+ * sum_i W(A(r,i)) * W(B(i,c)), while its sign, exponent and interval come from
+ * the scalar half of mp_mul and mp_add, computed step by step exactly as
+ * before.  gemm_prescale forms W(A) and W(B) once per call; the k chain adds
+ * their 62-bit products into 64-bit accumulators and folds them every few
+ * steps (2^32 mod m_i).  A step that rounds the product or the sum, whose
+ * sum's sign the bounds leave open (sign_estimate needs the residues), or
+ * whose exponents are large enough for the integer exponent arithmetic to wrap
+ * runs the full mp_mul + mp_add on residues recovered from the accumulators,
+ * D = (-1)^s * W * 2^-e, and re-encodes the result.  Results are the same
+ * bits as the step-by-step chain; the residue work per step drops from two
+ * modular products and the sign handling per modulus to one multiply-add.
  */
 /* every SM holds many product chains here and the FP64 pipe binds: the
  * interval evaluation runs in fixed point on the integer pipes (mp_device.cuh) */
@@ -87,7 +109,8 @@ template <int N> __device__ __forceinline__ void split_add(mp_t<N> &res, const m
     round_if_needed<N>(res);
 }
 
-/* Three 128-thread blocks per SM (at most 168 registers a thread): measured
+/* The step-by-step chain, for calls without room for the W(A), W(B) scratch.
+ * Three 128-thread blocks per SM (at most 168 registers a thread): measured
  * faster than two (255 registers) despite the spills, 94.8 against 108.0 ms at
  * 1024^3; four (128 registers) spill too much. */
 template <int N, int BX, int BY>
@@ -122,25 +145,304 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn(int m, int n, int k, SoA al
     store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
 }
 
+
+/* ----------------------- the lazy-residue k chain ------------------------ */
+
+/* 2^e mod m for any integer e (2^-1 = (m+1)/2 for the odd m), square and multiply */
+__device__ __forceinline__ uint32_t pow2mod(long long e, uint32_t m, uint32_t mu) {
+    uint32_t base = e >= 0 ? 2u : (m + 1u) / 2u;
+    unsigned long long k = e >= 0 ? (unsigned long long)e : 0ull - (unsigned long long)e;
+    uint32_t r = 1u;
+    while (k) {
+        if (k & 1u) r = mulmod(r, base, m, mu);
+        base = mulmod(base, base, m, mu);
+        k >>= 1;
+    }
+    return r;
+}
+
+/* v mod m for any 64-bit v: two folds by c32 = 2^32 mod m (v < 2^61 after
+ * them), then the Barrett step of mulmod */
+__device__ __forceinline__ uint32_t reduce64(uint64_t v, uint32_t m, uint32_t mu, uint32_t c32) {
+    v = (v >> 32) * c32 + (v & 0xffffffffull);
+    v = (v >> 32) * c32 + (v & 0xffffffffull);
+    uint32_t q = __umulhi((uint32_t)(v >> 30), mu);
+    uint32_t r = (uint32_t)v - q * m;
+    r = min(r, r - m);
+    r = min(r, r - m);
+    return r;
+}
+
+/* W = (-1)^s * d * 2^e mod m_i of one element, for every modulus */
+template <int N> __device__ __forceinline__ uint32_t encode_residue(int d, int s, long long e, int i) {
+    const Tables<N> &t = T<N>();
+    const uint32_t m = (uint32_t)t.moduli[i];
+    const uint32_t v = s ? (d ? m - (uint32_t)d : 0u) : (uint32_t)d;
+    return mulmod(v, pow2mod(e, m, t.mu[i]), m, t.mu[i]);
+}
+
+/* W(A) and W(B): A(r, c) of a rows x cols column-major matrix with leading
+ * dimension ld, stored for the k chain -- A_LAYOUT: int4 [c][N/4][rows] (the
+ * lanes of a warp, on consecutive rows, read 512 contiguous bytes); otherwise
+ * int4 [c][r][N/4] (a warp on one column of B reads one 128-byte row). */
+template <int N, bool A_LAYOUT>
+__global__ void __launch_bounds__(256) gemm_prescale(const int *digits, const int *sign, const int *exp, int ld,
+                                                     int rows, int cols, int4 *out) {
+    constexpr int Q = N / 4;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)rows * cols) return;
+    const int r = (int)(e % rows), c = (int)(e / rows);
+    const long long src = (long long)ld * c + r;
+    const int s = __ldg(sign + src), x = __ldg(exp + src);
+    const int4 *dp = reinterpret_cast<const int4 *>(digits + (size_t)src * N);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int4 d = __ldg(dp + q);
+        int4 w;
+        w.x = (int)encode_residue<N>(d.x, s, x, 4 * q);
+        w.y = (int)encode_residue<N>(d.y, s, x, 4 * q + 1);
+        w.z = (int)encode_residue<N>(d.z, s, x, 4 * q + 2);
+        w.w = (int)encode_residue<N>(d.w, s, x, 4 * q + 3);
+        const size_t o = A_LAYOUT ? ((size_t)c * Q + q) * rows + r : ((size_t)c * rows + r) * Q + q;
+        out[o] = w;
+    }
+}
+
+/* sign, exponent and interval of a number, without residues */
+struct Scal {
+    int sign, exp;
+    er_t ev[2];
+};
+
+/* the test of round_if_needed */
+template <int N> __device__ __forceinline__ bool needs_round(const er_t &u) {
+    const Tables<N> &t = T<N>();
+    return dnz(u.frac) && u.exp >= t.mp_h && (int)(u.exp - t.mp_h + 1) > 0;
+}
+
+/* The scalar half of mp_add (mp_device.cuh), the same expressions: the sum's
+ * sign, exponent and interval, and the flags that keep or drop each operand.
+ * Returns false when the signs of the bounds disagree: the sign then comes from
+ * sign_estimate, which needs the residues. */
+template <int N>
+__device__ __forceinline__ bool add_scalars(Scal &r, int &nzx_out, int &nzy_out, const Scal &x, const Scal &y) {
+    const Tables<N> &t = T<N>();
+    int ex = x.exp, ey = y.exp, sx = x.sign, sy = y.sign;
+    const int dexp = ex - ey;
+    int gamma = dexp > 0 ? dexp : 0;
+    int theta = dexp < 0 ? -dexp : 0;
+    const int nzx = (!dnz(y.ev[1].frac) || (theta + y.ev[1].exp) < t.mp_j);
+    const int nzy = (!dnz(x.ev[1].frac) || (gamma + x.ev[1].exp) < t.mp_j);
+    gamma *= nzy;
+    theta *= nzx;
+    ex = (ex - gamma) * nzx;
+    ey = (ey - theta) * nzy;
+    sx *= nzx;
+    sy *= nzy;
+    const int fx = (1 - 2 * sx) * nzx;
+    const int fy = (1 - 2 * sy) * nzy;
+    er_t ax[2], ay[2];
+    ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
+    ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
+    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
+    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
+    er_t ev[2];
+    ev[0] = er_add<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
+    ev[1] = er_add<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
+    const int sign = dneg(ev[0].frac);
+    const bool decided = sign == (int)dneg(ev[1].frac);
+    r.sign = sign;
+    r.exp = (ex == 0) ? ey : ex;
+    if (sign) {
+        r.ev[0].frac = -ev[1].frac; r.ev[0].exp = ev[1].exp;
+        r.ev[1].frac = -ev[0].frac; r.ev[1].exp = ev[0].exp;
+    } else {
+        r.ev[0] = ev[0];
+        r.ev[1] = ev[1];
+    }
+    nzx_out = nzx;
+    nzy_out = nzy;
+    return decided;
+}
+
+/* the residues D = (-1)^s * W * 2^-e mod m_i of a number from its accumulators */
+template <int N> __device__ __noinline__ void residues_from_acc(int *d, const uint64_t *w, int s, int e) {
+    const Tables<N> &t = T<N>();
+    for (int i = 0; i < N; i++) {
+        const uint32_t m = (uint32_t)t.moduli[i], mu = t.mu[i];
+        const uint32_t v = mulmod(reduce64(w[i], m, mu, t.pow2_32[i]), pow2mod(-(long long)e, m, mu), m, mu);
+        d[i] = (int)(s ? (v ? m - v : 0u) : v);
+    }
+}
+
+/* One step of the chain the general way: the full mp_mul and mp_add on the
+ * residues recovered from the accumulators w, then the result re-encoded. */
+template <int N>
+__device__ __noinline__ void full_step(uint64_t *w, Scal *sum, SoA A, long long ia, int lenA, SoA B, long long ib,
+                                       int lenB) {
+    mp_t<N> x, a, b, p, r;
+    x.sign = sum->sign;
+    x.exp = sum->exp;
+    x.ev[0] = sum->ev[0];
+    x.ev[1] = sum->ev[1];
+    residues_from_acc<N>(x.d, w, x.sign, x.exp);
+    load_soa<N>(a, A.digits, A.sign, A.exp, A.eval, lenA, ia);
+    load_soa<N>(b, B.digits, B.sign, B.exp, B.eval, lenB, ib);
+    mp_mul<N>(p, a, b);
+    mp_add<N>(r, x, p);
+    for (int i = 0; i < N; i++) w[i] = encode_residue<N>(r.d[i], r.sign, r.exp, i);
+    sum->sign = r.sign;
+    sum->exp = r.exp;
+    sum->ev[0] = r.ev[0];
+    sum->ev[1] = r.ev[1];
+}
+
+__device__ __forceinline__ bool small_exp(int e, int lim) { return e >= -lim && e <= lim; }
+
+/* Products added between two folds of the accumulators: after a fold an
+ * accumulator is below 2^32 * m < 2^62.3, each product below m^2 < 2^60.6
+ * (every predefined modulus is below 2^30.3), so six more stay below 2^64. */
+constexpr int kFoldEvery = 6;
+
+template <int N, int BX, int BY>
+__global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
+                                                       int ldb, SoA beta, int *cd, int *cs, int *ce, er_t *cv,
+                                                       const int *clen, int ldc, const int4 *WA, const int4 *WB) {
+    constexpr int Q = N / 4;
+    const Tables<N> &t = T<N>();
+    const int row = blockIdx.x * BX + threadIdx.x;
+    const int col = blockIdx.y * BY + threadIdx.y;
+    if (row >= m || col >= n) return;
+    const int lenA = __ldg(A.len), lenB = __ldg(B.len);
+    const longlong2 *aev = reinterpret_cast<const longlong2 *>(A.eval);
+    const longlong2 *bev = reinterpret_cast<const longlong2 *>(B.eval);
+    const int4 *wa = WA + row;
+    const int4 *wb = WB + (size_t)col * k * Q;
+    uint64_t acc[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) acc[i] = 0;
+    Scal sum;
+    sum.sign = 0;
+    sum.exp = 0;
+    sum.ev[0].frac = 0.0; sum.ev[0].exp = 0;
+    sum.ev[1].frac = 0.0; sum.ev[1].exp = 0;
+    int since_fold = 0;
+    for (int i = 0; i < k; i++) {
+        const long long ia = (long long)lda * i + row, ib = (long long)col * ldb + i;
+        int4 u[Q], v[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
+            v[q] = __ldg(wb + (size_t)i * Q + q);
+        }
+        const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
+        const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);
+        const longlong2 a0 = __ldg(aev + ia), a1 = __ldg(aev + lenA + ia);
+        const longlong2 b0 = __ldg(bev + ib), b1 = __ldg(bev + lenB + ib);
+        const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
+        const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
+        /* mp_mul without residues */
+        Scal p;
+        p.sign = sa ^ sb;
+        p.exp = ea + eb;
+        p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+        p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+        Scal r;
+        int nzx, nzy;
+        const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
+        const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
+                          small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
+        if (lazy) {
+            if (!nzx) {
+#pragma unroll
+                for (int j = 0; j < N; j++) acc[j] = 0;
+            }
+            if (nzy) {
+#pragma unroll
+                for (int q = 0; q < Q; q++) {
+                    acc[4 * q] += (uint64_t)(uint32_t)u[q].x * (uint32_t)v[q].x;
+                    acc[4 * q + 1] += (uint64_t)(uint32_t)u[q].y * (uint32_t)v[q].y;
+                    acc[4 * q + 2] += (uint64_t)(uint32_t)u[q].z * (uint32_t)v[q].z;
+                    acc[4 * q + 3] += (uint64_t)(uint32_t)u[q].w * (uint32_t)v[q].w;
+                }
+            }
+            sum = r;
+        } else {
+            uint64_t w[N]; /* copies: see round_if_needed */
+            Scal sc = sum;
+#pragma unroll
+            for (int j = 0; j < N; j++) w[j] = acc[j];
+            full_step<N>(w, &sc, A, ia, lenA, B, ib, lenB);
+#pragma unroll
+            for (int j = 0; j < N; j++) acc[j] = w[j];
+            sum = sc;
+        }
+        if (++since_fold == kFoldEvery) {
+            since_fold = 0;
+#pragma unroll
+            for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
+        }
+    }
+    mp_t<N> s;
+    {
+        uint64_t w[N];
+        int d[N];
+#pragma unroll
+        for (int j = 0; j < N; j++) w[j] = acc[j];
+        residues_from_acc<N>(d, w, sum.sign, sum.exp);
+#pragma unroll
+        for (int j = 0; j < N; j++) s.d[j] = d[j];
+    }
+    s.sign = sum.sign;
+    s.exp = sum.exp;
+    s.ev[0] = sum.ev[0];
+    s.ev[1] = sum.ev[1];
+    const int lenC = __ldg(clen);
+    const long long ic = (long long)col * ldc + row;
+    mp_t<N> al, be, buf, c0, cb, res;
+    load_soa<N>(al, alpha.digits, alpha.sign, alpha.exp, alpha.eval, __ldg(alpha.len), 0);
+    load_soa<N>(be, beta.digits, beta.sign, beta.exp, beta.eval, __ldg(beta.len), 0);
+    mp_mul<N>(buf, s, al);
+    load_soa<N>(c0, cd, cs, ce, cv, lenC, ic);
+    mp_mul<N>(cb, c0, be);
+    split_add<N>(res, cb, buf);
+    store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
+}
+
 template <int N>
 cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda, const mp_array_t &B,
-                int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc, cudaStream_t s) {
+                int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s) {
     constexpr int BX = 32, BY = 4;
     dim3 block(BX, BY), grid((m + BX - 1) / BX, (n + BY - 1) / BY);
-    gemm_nn<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta), C.digits,
-                                              C.sign, C.exp, reinterpret_cast<er_t *>(C.eval), C.len, ldc);
+    er_t *cv = reinterpret_cast<er_t *>(C.eval);
+    if (ws.ptr != nullptr && ws.bytes >= gemm_workspace_bytes(N, m, n, k)) {
+        int4 *wa = static_cast<int4 *>(ws.ptr);
+        int4 *wb = wa + (size_t)m * k * (N / 4);
+        const long long na = (long long)m * k, nb = (long long)k * n;
+        gemm_prescale<N, true><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A.digits, A.sign, A.exp, lda, m, k, wa);
+        gemm_prescale<N, false><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, wb);
+        gemm_nn_lazy<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta),
+                                                       C.digits, C.sign, C.exp, cv, C.len, ldc, wa, wb);
+    } else {
+        gemm_nn<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta), C.digits,
+                                                  C.sign, C.exp, cv, C.len, ldc);
+    }
     return cudaGetLastError();
 }
 
 } // namespace
 
+size_t gemm_workspace_bytes(int nmod, int m, int n, int k) {
+    return ((size_t)m * k + (size_t)k * n) * (size_t)nmod * 4;
+}
+
 cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
                         const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
-                        cudaStream_t s) {
+                        Workspace ws, cudaStream_t s) {
     switch (nmod) {
-    case 8: return run<8>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
-    case 16: return run<16>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
-    case 32: return run<32>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+    case 8: return run<8>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s);
+    case 16: return run<16>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s);
+    case 32: return run<32>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -39,9 +39,12 @@ cudaError_t launch_gemv(int nmod, bool trans, int m, int n, const mp_array_t &al
                         const mp_array_t &x, int incx, const mp_array_t &beta, const mp_array_t &y, int incy,
                         int b3, Workspace ws, cudaStream_t s);
 
+/* mp_gemm: W(A) and W(B), the signed residues scaled by 2^exp, go to ws
+ * (gemm_workspace_bytes); with a smaller ws the chain runs step by step */
+size_t gemm_workspace_bytes(int nmod, int m, int n, int k);
 cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
                         const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
-                        cudaStream_t s);
+                        Workspace ws, cudaStream_t s);
 
 /* SpMV: the row schedule (length-sorted order) goes to ws */
 size_t spmv_workspace_bytes(int m);

@@ -51,6 +51,7 @@ struct Tables {
     /* the host conversion (double -> mp_float_t) replayed on the device */
     double recip_rn[N];          /* 1.0 / m_i rounded to nearest, as the host computes it */
     const int *host_ceil_log2;   /* device: host_ceil_log2_table() */
+    uint32_t pow2_32[N];         /* 2^32 mod m_i: folds a 64-bit residue accumulator */
 };
 
 /* Host-side copy of every table in the reference's array shapes. */

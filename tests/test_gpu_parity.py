@@ -186,6 +186,57 @@ def test_gemm_wide_exponents_vs_oracle(gpu, oracle, n):
     eq(r, oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m))
 
 
+def _gemm_case(gpu, oracle, n, A, B, m, cols, k, rng):
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    r = run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m)
+    eq(r, oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m))
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_gemm_exact_cancellation_vs_oracle(gpu, oracle, n):
+    """Column pairs of A repeated and row pairs of B negated: every second step
+    of each k chain cancels the sum to exactly zero, so the bounds leave the
+    sign open and mp_add decides it from the residues (sign_estimate); some
+    entries are zero."""
+    m, cols, k = 33, 9, 48
+    rng = np.random.default_rng(helpers.SEED + 11 + n)
+    a = helpers.doubles(rng, m * k, -40, 40).reshape(k, m)
+    b = helpers.doubles(rng, k * cols, -40, 40).reshape(cols, k)
+    a[1::2, :] = a[0::2, :]
+    b[:, 1::2] = -b[:, 0::2]
+    a[5, :7] = 0.0
+    b[2, 3:] = 0.0
+    _gemm_case(gpu, oracle, n, gpu.set_d(n, a.ravel()), gpu.set_d(n, b.ravel()), m, cols, k, rng)
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_gemm_big_integer_operands_vs_oracle(gpu, oracle, n):
+    """Operands with wide residue integers (cubes of converted doubles, made by
+    the oracle's mp_mul): products and sums round inside the k chain."""
+    m, cols, k = 20, 12, 30
+    rng = np.random.default_rng(helpers.SEED + 13 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, -20, 20))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, -20, 20))
+    A = oracle.mul(n, A, oracle.mul(n, A, A))
+    B = oracle.mul(n, B, oracle.mul(n, B, B))
+    _gemm_case(gpu, oracle, n, A, B, m, cols, k, rng)
+
+
+@pytest.mark.parametrize("n", [8, 32])
+def test_gemm_huge_exponents_vs_oracle(gpu, oracle, n):
+    """Exponents of A raised and those of B lowered by 2^28 + 5 (the products
+    keep ordinary exponents): the integer exponent arithmetic of these steps is
+    near its range, so the chain runs them step by step."""
+    m, cols, k = 16, 8, 24
+    rng = np.random.default_rng(helpers.SEED + 17 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, -30, 30))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, -30, 30))
+    A["exp"][::3] += (1 << 28) + 5
+    B["exp"][::3] -= (1 << 28) + 5
+    _gemm_case(gpu, oracle, n, A, B, m, cols, k, rng)
+
+
 def test_gemm_transposed_is_not_supported(gpu):
     rec = gpu.set_d(8, np.ones(4))
     d = gpu.DeviceArray.from_host(8, rec)
