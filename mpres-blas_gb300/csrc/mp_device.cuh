@@ -45,7 +45,14 @@ constexpr uint64_t kBiasExpMask = 1023ull << 52;
 
 template <int N> __device__ __forceinline__ const Tables<N> &T();
 
-__device__ __forceinline__ uint64_t dbits(double d) { return (uint64_t)__double_as_longlong(d); }
+/* The bits of a double, through a move the optimiser cannot see through: tests
+ * written on the bits (zero, sign) stay integer instructions instead of being
+ * folded back into double comparisons, which occupy GB300's narrow FP64 pipe. */
+__device__ __forceinline__ uint64_t dbits(double d) {
+    uint64_t u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(d));
+    return u;
+}
 __device__ __forceinline__ double bdbl(uint64_t u) { return __longlong_as_double((long long)u); }
 /* x != 0 for a double (false for +0 and -0) */
 __device__ __forceinline__ bool dnz(double d) { return (dbits(d) << 1) != 0; }
