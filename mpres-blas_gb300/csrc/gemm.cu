@@ -86,8 +86,8 @@ template <int N> __device__ __forceinline__ void split_add(mp_t<N> &res, const m
     const int minus = dneg(lo.frac) && dneg(up.frac);
     res.sign = minus;
     if (minus) {
-        res.ev[0].frac = -up.frac; res.ev[0].exp = up.exp;
-        res.ev[1].frac = -lo.frac; res.ev[1].exp = lo.exp;
+        res.ev[0].frac = dflip(up.frac); res.ev[0].exp = up.exp;
+        res.ev[1].frac = dflip(lo.frac); res.ev[1].exp = lo.exp;
     } else {
         res.ev[0] = lo;
         res.ev[1] = up;
@@ -254,8 +254,8 @@ __device__ __forceinline__ bool add_scalars(Scal &r, int &nzx_out, int &nzy_out,
     r.sign = sign;
     r.exp = (ex == 0) ? ey : ex;
     if (sign) {
-        r.ev[0].frac = -ev[1].frac; r.ev[0].exp = ev[1].exp;
-        r.ev[1].frac = -ev[0].frac; r.ev[1].exp = ev[0].exp;
+        r.ev[0].frac = dflip(ev[1].frac); r.ev[0].exp = ev[1].exp;
+        r.ev[1].frac = dflip(ev[0].frac); r.ev[1].exp = ev[0].exp;
     } else {
         r.ev[0] = ev[0];
         r.ev[1] = ev[1];

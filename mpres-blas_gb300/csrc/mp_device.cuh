@@ -60,6 +60,8 @@ __device__ __forceinline__ bool dnz(double d) { return (dbits(d) << 1) != 0; }
 __device__ __forceinline__ bool dneg(double d) { return (dbits(d) >> 63) && dnz(d); }
 /* x > 0 for a non-NaN double */
 __device__ __forceinline__ bool dpos(double d) { return !(dbits(d) >> 63) && dnz(d); }
+/* -x: the sign bit flipped (what IEEE negation does), on the integer pipes */
+__device__ __forceinline__ double dflip(double x) { return bdbl(dbits(x) ^ kSign); }
 /* x * f for f in {-1, 0, 1}: exactly the IEEE product, computed on bits */
 __device__ __forceinline__ double dscale_sign(double x, int f) {
     uint64_t u = dbits(x);
@@ -710,7 +712,7 @@ __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<
         /* ev[sign] = +-unit_low, without indexing ev by a runtime value (which
          * would place ev in local memory) */
         if (sign) {
-            u.frac = -u.frac;
+            u.frac = dflip(u.frac);
             ev[1] = u;
         } else {
             ev[0] = u;
@@ -750,9 +752,9 @@ __device__ __forceinline__ void mp_add(mp_t<N> &r, const mp_t<N> &x, const mp_t<
     }
     if (sign) {
         er_t lo = ev[0];
-        ev[0].frac = -ev[1].frac;
+        ev[0].frac = dflip(ev[1].frac);
         ev[0].exp = ev[1].exp;
-        ev[1].frac = -lo.frac;
+        ev[1].frac = dflip(lo.frac);
         ev[1].exp = lo.exp;
     }
     r.ev[0] = ev[0];
