@@ -327,32 +327,38 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, S
     sum.ev[0].frac = 0.0; sum.ev[0].exp = 0;
     sum.ev[1].frac = 0.0; sum.ev[1].exp = 0;
     int since_fold = 0;
-    for (int i = 0; i < k; i++) {
-        const long long ia = (long long)lda * i + row, ib = (long long)col * ldb + i;
-        int4 u[Q], v[Q];
+    /* The k chain.  The inner loop runs the steps that stay lazy and leaves at
+     * the first that does not; that step runs out of line, then the loop
+     * resumes.  Keeping the call outside the inner loop keeps the loop free of
+     * the register saves around it (measured 4% of the time at 1024^3). */
+    int i = 0;
+    for (;;) {
+        for (; i < k; i++) {
+            const long long ia = (long long)lda * i + row, ib = (long long)col * ldb + i;
+            int4 u[Q], v[Q];
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
-            v[q] = __ldg(wb + (size_t)i * Q + q);
-        }
-        const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
-        const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);
-        const longlong2 a0 = __ldg(aev + ia), a1 = __ldg(aev + lenA + ia);
-        const longlong2 b0 = __ldg(bev + ib), b1 = __ldg(bev + lenB + ib);
-        const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
-        const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
-        /* mp_mul without residues */
-        Scal p;
-        p.sign = sa ^ sb;
-        p.exp = ea + eb;
-        p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
-        p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
-        Scal r;
-        int nzx, nzy;
-        const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
-        const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
-                          small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
-        if (lazy) {
+            for (int q = 0; q < Q; q++) {
+                u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
+                v[q] = __ldg(wb + (size_t)i * Q + q);
+            }
+            const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
+            const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);
+            const longlong2 a0 = __ldg(aev + ia), a1 = __ldg(aev + lenA + ia);
+            const longlong2 b0 = __ldg(bev + ib), b1 = __ldg(bev + lenB + ib);
+            const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
+            const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
+            /* mp_mul without residues */
+            Scal p;
+            p.sign = sa ^ sb;
+            p.exp = ea + eb;
+            p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+            p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+            Scal r;
+            int nzx, nzy;
+            const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
+            const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
+                              small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
+            if (!lazy) break;
             if (!nzx) {
 #pragma unroll
                 for (int j = 0; j < N; j++) acc[j] = 0;
@@ -367,12 +373,19 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, S
                 }
             }
             sum = r;
-        } else {
+            if (++since_fold == kFoldEvery) {
+                since_fold = 0;
+#pragma unroll
+                for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
+            }
+        }
+        if (i >= k) break;
+        {
             uint64_t w[N]; /* copies: see round_if_needed */
             Scal sc = sum;
 #pragma unroll
             for (int j = 0; j < N; j++) w[j] = acc[j];
-            full_step<N>(w, &sc, A, ia, lenA, B, ib, lenB);
+            full_step<N>(w, &sc, A, (long long)lda * i + row, lenA, B, (long long)col * ldb + i, lenB);
 #pragma unroll
             for (int j = 0; j < N; j++) acc[j] = w[j];
             sum = sc;
@@ -382,6 +395,7 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, S
 #pragma unroll
             for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
         }
+        i++;
     }
     mp_t<N> s;
     {
