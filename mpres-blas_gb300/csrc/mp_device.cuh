@@ -253,6 +253,26 @@ template <bool UP> __device__ __forceinline__ double div_by_const(double p, doub
  * p * 2^k - q0 * Z < 2Z fits 64 bits, and one comparison with Z corrects q0 and
  * yields the remainder that decides the directed rounding.  Other operands use
  * the FP64 intrinsics. */
+/* a * b = hi * 2^64 + lo for a, b < 2^53, from four 32-bit partial products
+ * that the high and the low half share */
+__device__ __forceinline__ void mul_wide53(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
+    const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+    const uint64_t p00 = (uint64_t)a0 * b0;
+    const uint64_t mid = (uint64_t)a0 * b1 + (uint64_t)a1 * b0 + (p00 >> 32); /* < 2^55 */
+    lo = (mid << 32) | (p00 & 0xffffffffull);
+    hi = (uint64_t)a1 * b1 + (mid >> 32);
+}
+/* the same for a < 2^53 and any 64-bit b: the middle sum may carry out of 64 bits */
+__device__ __forceinline__ void mul_wide53x64(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
+    const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), b0 = (uint32_t)b, b1 = (uint32_t)(b >> 32);
+    const uint64_t p00 = (uint64_t)a0 * b0, p10 = (uint64_t)a1 * b0;
+    const uint64_t mid = (uint64_t)a0 * b1 + (p00 >> 32); /* at most 2^64 - 2^32 */
+    const uint64_t mid2 = mid + p10;
+    const uint64_t carry = mid2 < p10 ? (1ull << 32) : 0ull;
+    lo = (mid2 << 32) | (p00 & 0xffffffffull);
+    hi = (uint64_t)a1 * b1 + (mid2 >> 32) + carry;
+}
+
 template <bool UP>
 __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z, double zr, uint64_t zinv) {
     constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
@@ -263,7 +283,8 @@ __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &
     if (ex == 1023u && ey == 1023u) {
         const bool up = UP != (sgn != 0); /* round the magnitude up */
         const uint64_t mx = (bx & kMant) | kHidden, my = (by & kMant) | kHidden;
-        const uint64_t hi = __umul64hi(mx, my), lo = mx * my; /* P in [2^104, 2^106) */
+        uint64_t hi, lo;
+        mul_wide53(mx, my, hi, lo); /* P in [2^104, 2^106) */
         const int sh = (hi >> 41) ? 53 : 52;
         uint64_t p = (hi << (64 - sh)) | (lo >> sh);
         p += (up && (lo & ((1ull << sh) - 1))) ? 1u : 0u;
@@ -276,7 +297,8 @@ __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &
         const uint64_t mz = (bz & kMant) | kHidden;
         const int ez = (int)((bz >> 52) & 2047) - 1023;
         const bool k52 = p >= mz;
-        const uint64_t thi = __umul64hi(p, zinv), tlo = p * zinv;
+        uint64_t thi, tlo;
+        mul_wide53x64(p, zinv, thi, tlo);
         uint64_t q = k52 ? thi : ((thi << 1) | (tlo >> 63));
         uint64_t rem = (k52 ? (p << 52) : (p << 53)) - q * mz;
         if (rem >= mz) {
