@@ -250,7 +250,10 @@ int mpres_gemv(int nmod, int trans, int m, int n, const mp_array_t *alpha, const
 /* cuda::mp_gemm<blockDim1x, blockDim1y, gridDim2x, gridDim2y, blockDim3>
  * (src/blas/gemm.cuh:69-168): C = alpha*A*B + beta*C, column-major, no-transpose
  * only (the reference prints and returns for the other cases; this returns
- * MPRES_ERR_NOT_SUPPORTED).  Launch parameters do not affect results. */
+ * MPRES_ERR_NOT_SUPPORTED).  Launch parameters do not affect results.  The
+ * signed, power-of-two-scaled residues of A and B, (m*k + k*n)*4*nmod bytes, go
+ * to the per-(device, stream) workspace; without room for them the same result
+ * comes from the slower step-by-step chain, which needs no scratch. */
 int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_array_t *alpha,
                const mp_array_t *A, int lda, const mp_array_t *B, int ldb, const mp_array_t *beta, mp_array_t *C,
                int ldc, mp_array_t *buffer, int blockDim1x, int blockDim1y, int gridDim2x, int gridDim2y,
