@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -685,7 +686,11 @@ int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_a
     if (!alpha || !A || !B || !beta || !C) return fail(MPRES_ERR_INVALID_VALUE, "mpres_gemm: null array");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Workspace ws;
-    if (workspace(s, gemm_workspace_bytes(nmod, m, n, k), ws) != MPRES_SUCCESS) {
+    /* MPRES_GEMM_NO_SCRATCH=1 selects the step-by-step chain, the path taken when
+     * the workspace cannot grow (same bits, no scratch) */
+    const char *no_scratch = std::getenv("MPRES_GEMM_NO_SCRATCH");
+    const bool scratch = !(no_scratch && no_scratch[0] == '1');
+    if (scratch && workspace(s, gemm_workspace_bytes(nmod, m, n, k), ws) != MPRES_SUCCESS) {
         ws = Workspace{}; /* no room for W(A), W(B): the step-by-step chain, no scratch */
         cudaGetLastError(); /* the failed allocation is not this call's error */
     }

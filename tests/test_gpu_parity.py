@@ -237,6 +237,22 @@ def test_gemm_huge_exponents_vs_oracle(gpu, oracle, n):
     _gemm_case(gpu, oracle, n, A, B, m, cols, k, rng)
 
 
+@pytest.mark.parametrize("n,lo,hi", [(8, -32, 32), (32, -32, 32), (16, -400, 400)])
+def test_gemm_without_scratch_vs_oracle(gpu, oracle, monkeypatch, n, lo, hi):
+    """MPRES_GEMM_NO_SCRATCH=1 selects the step-by-step k chain, the path mp_gemm
+    takes when its workspace cannot grow: the same bits as the lazy-residue chain."""
+    m, cols, k = 36, 20, 50
+    rng = np.random.default_rng(helpers.SEED + 19 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, lo, hi))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, lo, hi))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, lo, hi))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    want = oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m)
+    eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
+    monkeypatch.setenv("MPRES_GEMM_NO_SCRATCH", "1")
+    eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
+
+
 def test_gemm_transposed_is_not_supported(gpu):
     rec = gpu.set_d(8, np.ones(4))
     d = gpu.DeviceArray.from_host(8, rec)
