@@ -255,8 +255,9 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     sz = 4 * n + 40
     e2e = {"value": world * ops * e2e_steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": 3 * m * m * sz,
            "d2h_bytes_per_step": m * m * sz}
+    # per step: gemm_prescale for A and for B, then gemm_nn_lazy (the restore of C is a torch copy)
     return dict(secs=secs, value=value, roofline=roof, e2e=e2e, clocks=clk.summary(), host=host,
-                launches=steps)
+                launches=3 * steps)
 
 
 def bench_dot(torch, mp, stream, steps, warmup, world, hbm):
