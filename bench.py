@@ -8,9 +8,9 @@ C = alpha*A*B + beta*C with m = n = k = 1024, column-major, 32 moduli, entries
 u*2^e (u ~ U(-1,1), e ~ U{-32..32}), alpha, beta ~ U(-1,1); a step is one
 mp_gemm call.  `value` is MP ops/s (one MP op = one multiple-precision multiply
 or add; a GEMM step is 2*m*n*k + 3*m*n of them) with operands resident in HBM;
-`e2e` is the same through the C ABI with host mp_float_t buffers (the
-reference-facing mp_array_host2device / device2host copies inside the timed
-region).  The line also carries plain mp_dot (n = 2^20, 8 moduli) and
+`e2e` is the same through the C ABI with host mp_float_t buffers in pinned
+memory (the reference-facing mp_array_host2device / device2host copies inside
+the timed region).  The line also carries plain mp_dot (n = 2^20, 8 moduli) and
 mp_spmv_csr / csrv (2^20 rows, power-law row lengths, 8 moduli) measurements.
 
 --impl reference times the reference's CPU path for the same workload: the
@@ -200,6 +200,14 @@ def probe_rates(torch, mp, stream):
     return out
 
 
+def pinned_copy(torch, arr):
+    """A copy of a host record array in page-locked memory (allocated once,
+    outside any timed region), so host<->device copies run at DMA speed."""
+    buf = torch.empty(arr.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(arr.dtype)
+    buf[...] = arr
+    return buf
+
+
 def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     """C = alpha*A*B + beta*C, m = n = k = 1024, 32 moduli.  Every step starts
     from the same C, as the reference's own benchmark re-uploads C before each
@@ -235,14 +243,17 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
                          "arithmetic of each step binds",
             "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
 
-    # e2e: host mp_float_t arrays through the C ABI copies, every step
+    # e2e: host mp_float_t arrays in pinned memory through the C ABI copies, every step
+    pinned = {k: pinned_copy(torch, host[k]) for k in ("A", "B", "C")}
+    c_out = pinned_copy(torch, host["C"])
+
     def e2e_step():
-        d["A"].upload(host["A"])
-        d["B"].upload(host["B"])
-        d["C"].upload(host["C"])
+        d["A"].upload(pinned["A"])
+        d["B"].upload(pinned["B"])
+        d["C"].upload(pinned["C"])
         step()
         torch.cuda.synchronize()
-        d["C"].download()
+        d["C"].download(out=c_out)
 
     for _ in range(1):
         e2e_step()

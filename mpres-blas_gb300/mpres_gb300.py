@@ -293,8 +293,12 @@ class DeviceArray:
         check(lib().mpres_array_host2device(self.nmod, ctypes.byref(self.a), host.ctypes.data, self.size),
               "mpres_array_host2device")
 
-    def download(self):
-        out = np.zeros(self.size, mp_dtype(self.nmod))
+    def download(self, out=None):
+        """The records as a host array; `out` (e.g. a pinned buffer of this
+        size and record type) is filled and returned instead of a new array."""
+        if out is None:
+            out = np.zeros(self.size, mp_dtype(self.nmod))
+        assert out.dtype.itemsize == 4 * self.nmod + 40 and len(out) == self.size and out.flags.c_contiguous
         check(lib().mpres_array_device2host(self.nmod, out.ctypes.data, ctypes.byref(self.a), self.size),
               "mpres_array_device2host")
         return out
