@@ -36,8 +36,9 @@
  * bits as the step-by-step chain; the residue work per step drops from two
  * modular products and the sign handling per modulus to one multiply-add.
  */
-/* every SM holds many product chains here and the FP64 pipe binds: the
- * interval evaluation runs in fixed point on the integer pipes (mp_device.cuh) */
+/* every SM holds many product chains here and the FP64 pipe is narrow: the
+ * interval evaluation (out-of-line steps, epilogue, step-by-step chain) runs in
+ * fixed point on the integer pipes (mp_device.cuh) */
 #define MPRES_EVAL_FIXED_POINT 1
 #include "kernels.h"
 #include "mp_device.cuh"
