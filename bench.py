@@ -200,6 +200,12 @@ def probe_rates(torch, mp, stream):
     return out
 
 
+def gemm_config(world):
+    """The headline workload, named the same by both arms."""
+    return {"workload": "mp_gemm m=n=k=1024, 32 moduli (params.32_32bit), NN, column-major", "global_batch": 1,
+            "seq_len": None, "parallelism": "replicas" if world > 1 else "single"}
+
+
 def pinned_copy(torch, arr):
     """A copy of a host record array in page-locked memory (allocated once,
     outside any timed region), so host<->device copies run at DMA speed."""
@@ -663,8 +669,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32 residues + f64 interval bounds",
             "data": "synthetic (seeded)",
-            "config": {"workload": "mp_gemm m=n=k=1024, 32 moduli, NN, column-major", "global_batch": 1,
-                       "seq_len": None, "parallelism": "replicas"},
+            "config": gemm_config(world),
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "MP ops/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}))
         return
@@ -699,10 +704,8 @@ def main():
         "warmup": max(3, args.warmup), "ms_per_step": g["secs"] / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32 residues + f64 interval bounds",
         "data": "synthetic (seeded u*2^e entries; the reference publishes no dataset)",
-        "config": {"workload": "mp_gemm m=n=k=1024, 32 moduli (params.32_32bit), NN, column-major",
-                   "global_batch": 1, "seq_len": None, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (3 x 176 MB)",
-                   "c_per_step": "C restored from its initial value by a device copy inside each timed step"},
+        "config": dict(gemm_config(world), l2="inputs larger than L2 (3 x 176 MB)",
+                       c_per_step="C restored from its initial value by a device copy inside each timed step"),
         "roofline": g["roofline"], "hbm_peak_source": peak_src, "e2e": g["e2e"], "clocks": g["clocks"],
         "gpu_launches": g["launches"],
     }
