@@ -140,6 +140,39 @@ def test_random_blas_matches_reference(oracle):
     eq(oracle.spmv_csrv(8, 400, 8, irp, ja, vals, xv), R.spmv_csrv(400, 8, irp, ja, vals, xv))
 
 
+@needs_ref
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_gemm_edge_inputs_match_reference(oracle, n):
+    """Two GEMM input classes the GPU parity tests use for the out-of-line steps
+    of the lazy-residue chain: exact cancellations (the sum's sign comes from the
+    residues) and cubed operands (products and sums round), with zeros.  The
+    oracle must equal the reference here too.  Wide or huge exponent ranges are
+    compared with the oracle only: at the first step of a chain the running sum
+    is zero, and the reference aligns it by indexing RNS_POW2 with the full
+    exponent gap, past the end of the table (the CPU build faults there); the
+    oracle and the CUDA kernels clamp that row, which gives the same product
+    because the zero's digits are all zero."""
+    if not ffi.ref_available(n):
+        pytest.skip("reference for %d moduli not built here" % n)
+    R = ffi.reference(n)
+    rng = np.random.default_rng(helpers.SEED + 700 + n)
+    m, cols, k = 12, 7, 26
+    al, be = R.set_d(rng.uniform(-1, 1, 1)), R.set_d(rng.uniform(-1, 1, 1))
+    for case in ("cancel", "cube"):
+        a = helpers.doubles(rng, m * k, -30, 30).reshape(k, m)
+        b = helpers.doubles(rng, k * cols, -30, 30).reshape(cols, k)
+        if case == "cancel":
+            a[1::2, :] = a[0::2, :]
+            b[:, 1::2] = -b[:, 0::2]
+        a[3, :4] = 0.0
+        A, B = R.set_d(a.ravel()), R.set_d(b.ravel())
+        if case == "cube":
+            A = R.mul(A, R.mul(A, A))
+            B = R.mul(B, R.mul(B, B))
+        C = R.set_d(helpers.doubles(rng, m * cols, -30, 30))
+        eq(oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m), R.gemm(m, cols, k, al, A, m, B, k, be, C, m))
+
+
 def test_dot_accuracy_within_reference_bound(oracle):
     """|r - exact| <= u*n/(1-u*n) * sum|x_i y_i|, u = 4/sqrt(M): the bound of the
     reference's accuracy test (tests/blas/accuracy/test_dot_accuracy.cu:39-90)."""
