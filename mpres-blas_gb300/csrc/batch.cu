@@ -273,11 +273,13 @@ int shape_slot(int nmod) {
     return si * 64 + (dev >= 0 && dev < 64 ? dev : 0);
 }
 
-/* the kernel's shared-memory limit, raised once per process for each variant */
+/* the kernel's shared-memory limit, raised on each device that runs a variant */
 template <int N, int MAXT> cudaError_t set_attr() {
-    static cudaError_t done = cudaFuncSetAttribute(batch_kernel<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   MAXT * (int)sizeof(mp_t<N>));
-    return done;
+    static PerDevice<cudaError_t> attrs(cuda_ok);
+    return attrs.get(current_device(), cudaErrorInvalidDevice, [] {
+        return cudaFuncSetAttribute(batch_kernel<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    MAXT * (int)sizeof(mp_t<N>));
+    });
 }
 
 template <int N, int MAXT> int occupancy(int threads) {

@@ -103,14 +103,18 @@ template <int N, int MAXT>
 cudaError_t run_shape(int n, const mp_array_t &x, int incx, const mp_array_t &y, int incy, const mp_array_t &r,
                       int g3, int b3, Workspace ws, cudaStream_t s) {
     const size_t smem = (size_t)b3 * sizeof(mp_t<N>);
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaFuncSetAttribute(dot_pass1<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAXT * sizeof(mp_t<N>));
-        cudaFuncSetAttribute(dot_pass2<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize, MAXT * sizeof(mp_t<N>));
-        attr_done = true;
-    }
+    /* the shared-memory limit of both passes, raised on each device that runs them */
+    static PerDevice<cudaError_t> attrs(cuda_ok);
+    cudaError_t e = attrs.get(current_device(), cudaErrorInvalidDevice, [] {
+        cudaError_t r = cudaFuncSetAttribute(dot_pass1<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             MAXT * sizeof(mp_t<N>));
+        if (r != cudaSuccess) return r;
+        return cudaFuncSetAttribute(dot_pass2<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    MAXT * sizeof(mp_t<N>));
+    });
+    if (e != cudaSuccess) return e;
     dot_pass1<N, MAXT><<<g3, b3, smem, s>>>(n, soa(x), incx, soa(y), incy, ws.ptr);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     dot_pass2<N, MAXT><<<1, b3, smem, s>>>(g3, ws.ptr, r.digits, r.sign, r.exp, reinterpret_cast<er_t *>(r.eval),
                                            r.len);
@@ -132,22 +136,23 @@ cudaError_t run(int n, const mp_array_t &x, int incx, const mp_array_t &y, int i
  * is a stand-in, not a device address: the address comes from
  * cudaGetSymbolAddress, once per device, with that device current. */
 __device__ __align__(256) unsigned char g_dot_noalloc_scratch[MPRES_DOT_NOALLOC_MAX_BLOCKS * (4 * 32 + 40)];
-void *g_noalloc_addr[64];
+
+bool nonnull(void *const &p) { return p != nullptr; }
 
 } // namespace
 
 cudaError_t dot_noalloc_scratch(Workspace &ws) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_dot_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_addr[dev] = p;
-    }
-    ws.ptr = g_noalloc_addr[dev];
+    static PerDevice<void *> addrs(nonnull);
+    const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    cudaError_t e = cudaSuccess;
+    void *p = addrs.get(dev, nullptr, [&e] {
+        void *a = nullptr;
+        e = cudaGetSymbolAddress(&a, g_dot_noalloc_scratch);
+        return e == cudaSuccess ? a : nullptr;
+    });
+    if (!p) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+    ws.ptr = p;
     ws.bytes = sizeof(g_dot_noalloc_scratch);
     return cudaSuccess;
 }

@@ -117,12 +117,13 @@ cudaError_t sums(int m, int n, const mp_array_t &A, int lda, const void *buf1, c
     const int outs = TRANS ? n : m;
     const int grid = (outs + R - 1) / R;
     const size_t smem = (size_t)threads * sizeof(mp_t<N>);
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaFuncSetAttribute(gemv_sums<N, MAXT, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             MAXT * sizeof(mp_t<N>));
-        attr_done = true;
-    }
+    /* the shared-memory limit, raised on each device that runs the kernel */
+    static PerDevice<cudaError_t> attrs(cuda_ok);
+    cudaError_t e = attrs.get(current_device(), cudaErrorInvalidDevice, [] {
+        return cudaFuncSetAttribute(gemv_sums<N, MAXT, TRANS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    MAXT * sizeof(mp_t<N>));
+    });
+    if (e != cudaSuccess) return e;
     gemv_sums<N, MAXT, TRANS><<<grid, threads, smem, s>>>(m, n, soa(A), lda, buf1, soa(beta), y.digits, y.sign, y.exp,
                                                           reinterpret_cast<er_t *>(y.eval), y.len, incy, b3, R);
     return cudaGetLastError();

@@ -8,9 +8,18 @@
 #include <cuda_runtime.h>
 
 #include "../../include/mpres_gb300.h"
+#include "per_device.h"
 #include "tables.h"
 
 namespace mpres {
+
+/* the current device ordinal, -1 if it cannot be read */
+inline int current_device() {
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess ? dev : -1;
+}
+inline bool cuda_ok(const cudaError_t &e) { return e == cudaSuccess; }
+inline bool positive(const int &v) { return v > 0; }
 
 cudaError_t upload_tables_dot(int n, const void *tab);
 cudaError_t upload_tables_gemv(int n, const void *tab);
@@ -67,6 +76,8 @@ cudaError_t launch_pack(int nmod, bool to_soa, void *aos, const mp_array_t &a, l
 
 cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, void *r, long long count,
                                cudaStream_t s);
+cudaError_t launch_chain_probe(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
+                               unsigned *rounds, void *res, cudaStream_t s);
 cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,
                              cudaStream_t s);
 cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void *out, long long count,

@@ -215,17 +215,19 @@ int grid_for(int work, int threads) {
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
-/* persistent grid: as many blocks as fit on the device */
+/* persistent grid: as many blocks as fit on the current device (computed
+ * once per device and kernel) */
 template <class K> int persistent_grid(K kernel, int threads) {
-    static int cached = 0;
-    if (!cached) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
-        cached = sms * (per_sm > 0 ? per_sm : 1);
-    }
-    return cached;
+    static PerDevice<int> grids(positive);
+    const int dev = current_device();
+    const int g = grids.get(dev, 0, [&] {
+        int sms = 0, per_sm = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess)
+            return 0;
+        return sms * (per_sm > 0 ? per_sm : 1);
+    });
+    return g > 0 ? g : 152;
 }
 
 Sched carve(Workspace ws, int m) {

@@ -8,7 +8,7 @@ RNS_EVAL_RELATIVE_ERROR and RNS_MODULI_VALUES.  This script copies those values,
 unchanged, into one C header so that the library can hold several sets at once.
 
 Run it where the reference checkout exists:
-    python gen_moduli_sets.py [path/to/reference/src]
+    python gen_moduli_sets.py <path to the reference checkout>/src
 The generated header is committed; the build never runs this script.
 """
 import pathlib
@@ -38,7 +38,9 @@ def parse(path):
 
 
 def main():
-    src = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    if len(sys.argv) < 2:
+        sys.exit("usage: gen_moduli_sets.py <reference src/ directory>")
+    src = pathlib.Path(sys.argv[1])
     sets = []
     for p in sorted((src / "params" / "32-bit-moduli").glob("params.*_32bit.h"),
                     key=lambda p: int(p.name.split(".")[1].split("_")[0])):

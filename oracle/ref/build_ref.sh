@@ -5,11 +5,18 @@
 # Needs the reference sources (REF_SRC, default /root/reference/src) and the
 # GMP/MPFR runtime libraries; the headers for those come from oracle/ref/shim.
 # Test infrastructure only: the output pins the oracle and makes golden vectors.
+# This recipe is the one place that names the checkout's location:
+#   build_ref.sh --where   prints the checkout root and exits 0, or exits 1 when
+#                          the sources are absent (the GPU machine has none).
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 ORACLE="$(dirname "$HERE")"
 REF_SRC="${REF_SRC:-/root/reference/src}"
 OUT="$ORACLE/_ref"
+if [ "${1:-}" = "--where" ]; then
+    if [ -d "$REF_SRC" ]; then dirname "$REF_SRC"; exit 0; fi
+    exit 1
+fi
 if [ ! -d "$REF_SRC" ]; then
     echo "reference sources not found at $REF_SRC; skipping oracle/_ref" >&2
     exit 0

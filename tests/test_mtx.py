@@ -12,7 +12,8 @@ import pytest
 import helpers
 from oracle import ffi
 
-LF10 = pathlib.Path("/root/reference/tests/sparse/matrices/LF10.mtx")
+_ROOT = ffi.reference_root()
+LF10 = (_ROOT / "tests" / "sparse" / "matrices" / "LF10.mtx") if _ROOT else pathlib.Path("LF10.mtx.absent")
 
 
 def write_mtx(path, m, n, entries, symmetric=False, dtype="real", comments=2):

@@ -21,13 +21,21 @@ def _call_noalloc(lib, n, count, x, y, r, g3, b3):
     return lib.lib().mpres_dot_noalloc(n, count, x.ref, 1, y.ref, 1, r.ref, g3, b3, None)
 
 
-def test_dot_noalloc_matches_dot_twice(gpu):
+# (moduli, count, gridDim3, blockDim3); the last case of the 32-moduli set
+# writes all 4096 block sums of the largest record size, the whole static array
+CASES = {
+    8: [(200000, 256, 64), (77777, 4096, 32)],
+    16: [(120001, 256, 64), (50000, 1000, 128)],
+    32: [(60013, 96, 32), (200000, 4096, 1024)],
+}
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_dot_noalloc_matches_dot_twice(gpu, n):
     import torch
-    n = 8
-    rng = np.random.default_rng(helpers.SEED + 4242)
-    cases = [(200000, 256, 64), (77777, 4096, 32)]
+    rng = np.random.default_rng(helpers.SEED + 4242 + n)
     data = []
-    for count, g3, b3 in cases:
+    for count, g3, b3 in CASES[n]:
         mx = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
         my = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
         x, y = gpu.DeviceArray.from_host(n, mx), gpu.DeviceArray.from_host(n, my)
