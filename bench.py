@@ -8,14 +8,23 @@ C = alpha*A*B + beta*C with m = n = k = 1024, column-major, 32 moduli, entries
 u*2^e (u ~ U(-1,1), e ~ U{-32..32}), alpha, beta ~ U(-1,1); a step is one
 mp_gemm call.  `value` is MP ops/s (one MP op = one multiple-precision multiply
 or add; a GEMM step is 2*m*n*k + 3*m*n of them) with operands resident in HBM;
-`e2e` is the same through the C ABI with host mp_float_t buffers in pinned
-memory (the reference-facing mp_array_host2device / device2host copies inside
-the timed region).  The line also carries plain mp_dot (n = 2^20, 8 moduli) and
-mp_spmv_csr / csrv (2^20 rows, power-law row lengths, 8 moduli) measurements.
+`e2e` is the same metric through the C ABI from host mp_float_t buffers in
+pinned memory: every step uploads A, B and C (mp_array_host2device), runs
+mp_gemm and downloads the product C (mp_array_device2host).  The line also
+carries plain mp_dot (n = 2^20, 8 moduli) and mp_spmv_csr / csrv (tpr 4, 16,
+32) / ell (2^20 rows, power-law row lengths, 8 moduli), each with its
+roofline, e2e and CPU baselines, the batched GEMV form and the serving loop.
 
---impl reference times the reference's CPU path for the same workload: the
-oracle port (oracle/, a restatement of the reference's arithmetic) on all host
-cores, on a bounded sample of the GEMM, extrapolated to MP ops/s.
+CPU baselines, timed on this host's cores on bounded samples of the same
+workloads: `cpu_baseline` is the reference's own CPU path, its MPFR loops with
+OpenMP at MP_PRECISION bits (oracle/mpfr_blas.c: mpfr_gemm, mpfr_dot,
+mpfr_mpspmv_csr), kind "mpfr"; `cpu_baseline_port` is the oracle's C
+restatement of the reference's multiple-precision arithmetic (the host
+mp_float_t loop), kind "port".
+
+--impl reference times the reference's CPU path for the headline workload (the
+MPFR mpfr_gemm loop on all host cores, a bounded block of C per step; the port
+where the host has no MPFR runtime).  It loads nothing of the CUDA library.
 
 Multi-GPU (torchrun): the path does not shard (a GEMM's outputs are independent
 but the benchmark does not split one); every rank runs an independent replica
@@ -157,12 +166,20 @@ def barrier(world):
 
 # --------------------------------------------------------------- workloads --
 
-def gemm_inputs(mp, n=32, m=1024):
+def gemm_doubles(m=1024):
+    """The headline GEMM's seeded entries as doubles (A, B, C, alpha, beta)."""
     rng = np.random.default_rng(SEED + 1)
-    host = {k: mp.set_d(n, doubles(rng, m * m, -32, 32)) for k in ("A", "B", "C")}
-    host["alpha"] = mp.set_d(n, rng.uniform(-1, 1, 1))
-    host["beta"] = mp.set_d(n, rng.uniform(-1, 1, 1))
-    return host
+    d = {k: doubles(rng, m * m, -32, 32) for k in ("A", "B", "C")}
+    d["alpha"] = rng.uniform(-1, 1, 1)
+    d["beta"] = rng.uniform(-1, 1, 1)
+    return d
+
+
+def gemm_inputs(set_d, n=32, m=1024):
+    """mp_float_t records of the headline GEMM, converted by set_d(n, doubles)
+    (the library's host mp_set_d, or the oracle's in the reference arm)."""
+    src = gemm_doubles(m)
+    return {k: set_d(n, v) for k, v in src.items()}, src
 
 
 def time_steps(torch, stream, fn, steps, warmup, world):
@@ -201,9 +218,11 @@ def probe_rates(torch, mp, stream):
 
 
 def gemm_config(world):
-    """The headline workload, named the same by both arms."""
+    """The headline workload, named identically by both arms."""
     return {"workload": "mp_gemm m=n=k=1024, 32 moduli (params.32_32bit), NN, column-major", "global_batch": 1,
-            "seq_len": None, "parallelism": "replicas" if world > 1 else "single"}
+            "seq_len": None, "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (3 x 176 MB)",
+            "c_per_step": "every step starts from the same C (device copy in the resident timing, upload in e2e)"}
 
 
 def pinned_copy(torch, arr):
@@ -214,15 +233,33 @@ def pinned_copy(torch, arr):
     return buf
 
 
+def e2e_time(torch, fn, steps, warmup, world):
+    """Wall seconds (max over ranks) of `steps` calls of fn after `warmup`
+    untimed ones; each call is synchronous (uploads, the operation, the read of
+    its result), so the host clock brackets the device work."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        fn()
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    barrier(world)
+    return max_over_ranks(secs, world)
+
+
 def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     """C = alpha*A*B + beta*C, m = n = k = 1024, 32 moduli.  Every step starts
     from the same C, as the reference's own benchmark re-uploads C before each
     timed call (tests/blas/performance/test_gemm_performance.cu): C accumulated
     over steps would grow its residue representation by the bits of beta each
-    time and make the later steps round in the epilogue.  The restore is a
-    device-to-device copy inside the timed region."""
+    time and make the later steps round in the epilogue.  In the resident timing
+    the restore is a device-to-device copy inside the timed region; in e2e C is
+    uploaded from the host every step and the product downloaded."""
     n, m = 32, 1024
-    host = gemm_inputs(mp, n, m)
+    host, src = gemm_inputs(mp.set_d, n, m)
     d = {k: mp.DeviceArray.from_host(n, v) for k, v in host.items()}
     c_work, c_init = mp.TensorArray(n, m * m), mp.TensorArray(n, m * m)
     c_init.upload(host["C"])
@@ -237,6 +274,7 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     secs = max_over_ranks(secs, world)
     ops = 2.0 * m * m * m + 3.0 * m * m
     value = world * ops * steps / secs
+    resident_c = c_work.download()
     rates = probe_rates(torch, mp, stream)
     w_int = 3.0 * m * m * m * n  # Barrett products per launch (1 in the multiply, 2 in the aligned add)
     per_launch = secs / steps
@@ -249,7 +287,8 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
                          "arithmetic of each step binds",
             "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
 
-    # e2e: host mp_float_t arrays in pinned memory through the C ABI copies, every step
+    # e2e: host mp_float_t arrays in pinned memory through the C ABI copies,
+    # every step: upload A, B, C; mp_gemm into C; download the product
     pinned = {k: pinned_copy(torch, host[k]) for k in ("A", "B", "C")}
     c_out = pinned_copy(torch, host["C"])
 
@@ -257,30 +296,68 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
         d["A"].upload(pinned["A"])
         d["B"].upload(pinned["B"])
         d["C"].upload(pinned["C"])
-        step()
-        torch.cuda.synchronize()
+        mp.gemm(n, m, m, m, d["alpha"], d["A"], m, d["B"], m, d["beta"], d["C"], m, stream=stream)
+        stream.synchronize()
         d["C"].download(out=c_out)
 
-    for _ in range(1):
-        e2e_step()
-    barrier(world)
-    t0 = time.perf_counter()
-    e2e_steps = max(1, min(steps, 3))
-    for _ in range(e2e_steps):
-        e2e_step()
-    e2e_secs = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_secs = e2e_time(torch, e2e_step, steps, 1, world)
     sz = 4 * n + 40
-    e2e = {"value": world * ops * e2e_steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": 3 * m * m * sz,
-           "d2h_bytes_per_step": m * m * sz}
+    e2e = {"value": world * ops * steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": 3 * m * m * sz,
+           "d2h_bytes_per_step": m * m * sz, "steps": steps,
+           "result_matches_resident": bool(c_out.tobytes() == resident_c.tobytes())}
     # per step: gemm_prescale for A and for B, then gemm_nn_lazy (the restore of C is a torch copy)
-    return dict(secs=secs, value=value, roofline=roof, e2e=e2e, clocks=clk.summary(), host=host,
+    return dict(secs=secs, value=value, roofline=roof, e2e=e2e, clocks=clk.summary(), host=host, src=src,
                 launches=3 * steps)
 
 
-def bench_dot(torch, mp, stream, steps, warmup, world, hbm):
+def chain_cycles(mp, n, kind, x, y, length):
+    """Per-step SM cycles of one warp's chains run alone (mpres_probe_chain),
+    best of three runs, with the steps' rounding counts."""
+    best = None
+    for _ in range(3):
+        cyc, pr, sr, _ = mp.probe_chain(n, kind, x, y, length)
+        if best is None or cyc.sum() < best[0].sum():
+            best = (cyc, pr, sr)
+    return best
+
+
+def dot_floor(mp, mx, my, count, g3, b3, mhz):
+    """Latency floor of mp_dot under the order key (g3, b3): the longest of a
+    few warps' 32 chains of count/(g3*b3) fused steps (chains exactly as pass 1
+    forms them), then the pass-1 tree, pass 2's chains of g3/b3 additions and
+    its tree, at the add-only step latency; SM cycles at `mhz`."""
+    K = g3 * b3
+    steps = -(-count // K)
+    chain = []
+    for blk in (0, g3 // 3, (2 * g3) // 3, g3 - 1):
+        lanes = blk * b3 + np.arange(32)
+        idx = (lanes[:, None] + K * np.arange(steps)[None, :]).ravel()
+        ok = idx < count
+        idx = np.where(ok, idx, 0)
+        cyc, pr, sr = chain_cycles(mp, 8, 0, mx[idx], my[idx], steps)
+        chain.append((int(cyc.sum()), float((sr > 0).mean()), float(sr.sum() / (32.0 * steps))))
+    # additions of partial sums: products summed pairwise, as the trees do
+    pr8 = mp.elementwise(8, mp.OP_MUL, mx[: 32 * 64], my[: 32 * 64])
+    acyc, _, asr = chain_cycles(mp, 8, 1, pr8, None, 64)
+    add_step = float(acyc.mean())
+    levels = int(np.ceil(np.log2(max(b3, 2))))
+    tree = (levels + -(-g3 // b3) + levels) * add_step
+    worst = max(c[0] for c in chain)
+    cycles = worst + tree
+    return {"floor_ms": cycles / (mhz * 1e3), "chain_cycles_worst_warp": worst, "steps": steps,
+            "step_cycles_mean": worst / steps, "add_step_cycles_mean": add_step,
+            "warp_steps_with_a_rounding": max(c[1] for c in chain), "lane_rounding_rate": chain[0][2],
+            "sm_mhz": mhz, "method": "mpres_probe_chain: one warp alone, clock64 per step, best of 3; "
+                                     "chain of the longest of 4 sampled warps + 2*log2(b3) + g3/b3 add steps"}
+
+
+def bench_dot(torch, mp, stream, steps, warmup, world, hbm, mhz=None):
+    """plain mp_dot, n = 2^20, 8 moduli, the reference benchmark's order
+    <512,128,8192,256,64> (tests/blas/performance/test_dot_performance.cu:35-39)."""
     n, count = 8, 1 << 20
     rng = np.random.default_rng(SEED + 0)
-    mx, my = mp.set_d(n, doubles(rng, count, -16, 16)), mp.set_d(n, doubles(rng, count, -16, 16))
+    xd, yd = doubles(rng, count, -16, 16), doubles(rng, count, -16, 16)
+    mx, my = mp.set_d(n, xd), mp.set_d(n, yd)
     x, y, r = mp.DeviceArray.from_host(n, mx), mp.DeviceArray.from_host(n, my), mp.DeviceArray(n, 1)
     order = (512, 128, 8192, 256, 64)
 
@@ -289,37 +366,153 @@ def bench_dot(torch, mp, stream, steps, warmup, world, hbm):
 
     secs = max_over_ranks(time_steps(torch, stream, step, steps, warmup, world), world)
     per = secs / steps
+    resident_r = r.download()
     algo = 2 * count * (4 * n + 40)
+    px, py, pr = pinned_copy(torch, mx), pinned_copy(torch, my), pinned_copy(torch, mx[:1])
+
+    def e2e_step():
+        x.upload(px)
+        y.upload(py)
+        mp.dot(n, count, x, y, r, order=order, stream=stream)
+        stream.synchronize()
+        r.download(out=pr)
+
+    e2e_secs = e2e_time(torch, e2e_step, steps, 1, world)
+    floor = dot_floor(mp, mx, my, count, order[3], order[4], mhz or 2070.0)
+    floor["achieved_over_floor"] = per * 1e3 / floor["floor_ms"]
     return {"workload": "mp_dot n=2^20, 8 moduli, order <512,128,8192,256,64>", "value": world * 2 * count / per,
-            "unit": "MP ops/s", "ms_per_step": per * 1e3, "launches": 2 * steps,
+            "chain_floor": floor,
+            "unit": "MP ops/s", "ms_per_step": per * 1e3, "steps": steps, "launches": 2 * steps,
             "roofline": {"bound": "hbm", "achieved": algo / per / 1e9, "peak": hbm, "unit": "GB/s",
                          "frac": algo / per / 1e9 / hbm, "traffic": traffic("dot_pass1")},
-            "data": (mx, my)}
+            "e2e": {"value": world * 2 * count * steps / e2e_secs, "unit": "MP ops/s",
+                    "h2d_bytes_per_step": 2 * count * (4 * n + 40), "d2h_bytes_per_step": 4 * n + 40,
+                    "result_matches_resident": bool(pr.tobytes() == resident_r.tobytes())},
+            "data": (xd, yd, mx, my)}
 
 
-def bench_spmv(torch, mp, stream, steps, warmup, world, hbm):
+def ell_on_device(torch, mp, m, irp, ja, vals):
+    """The ELLPACK form of a CSR matrix built on the device (column-major
+    slots col*m + row, zero padded; the reference's build_ell layout)."""
+    irp_t = torch.from_numpy(irp.astype(np.int64)).cuda()
+    lens = irp_t[1:] - irp_t[:-1]
+    maxnzr = int(lens.max().item())
+    nnz = int(irp[-1])
+    rows = torch.repeat_interleave(torch.arange(m, device="cuda"), lens)
+    slot = (torch.arange(nnz, device="cuda") - irp_t[:-1][rows]) * m + rows
+    del rows
+    ell_ja = torch.zeros(maxnzr * m, dtype=torch.int32, device="cuda")
+    ell_ja[slot] = torch.from_numpy(ja).cuda()
+    ell_as = torch.zeros(maxnzr * m, dtype=torch.float64, device="cuda")
+    ell_as[slot] = torch.from_numpy(vals).cuda()
+    del slot
+    return mp.DeviceEll.from_tensors(m, maxnzr, ell_ja, ell_as)
+
+
+def spmv_floor(mp, irp, ja, vals, mx, mhz):
+    """Latency floors of the SpMV kernels: a row is one chain (CSR, ELL) or
+    tpr lane-strided chains and a log2(tpr)-level tree (CSRV), so no schedule
+    finishes before the longest row's chain.  Measured on the warp holding the
+    32 longest rows (kind 2 chains, one warp alone), scaled to the longest
+    length; CSRV32 on the 32 lane chains of the longest row."""
+    lens = np.diff(irp)
+    order = np.argsort(lens)[::-1][:32]
+    L = int(lens[order].min())
+    Lmax = int(lens[order[0]])
+    idx = np.concatenate([np.arange(irp[r], irp[r] + L) for r in order])
+    cyc, _, sr = chain_cycles(mp, 8, 2, mx[ja[idx]], vals[idx], L)
+    step = float(cyc.mean())
+    r0 = int(order[0])
+    sub = -(-Lmax // 32)
+    lane_idx = np.array([[irp[r0] + l + 32 * t if l + 32 * t < Lmax else irp[r0] + l for t in range(sub)]
+                         for l in range(32)]).ravel()
+    cyc32, _, _ = chain_cycles(mp, 8, 2, mx[ja[lane_idx]], vals[lane_idx], sub)
+    pr8 = mp.elementwise(8, mp.OP_MUL, mx[: 32 * 64], mx[32 * 64: 64 * 64])
+    acyc, _, _ = chain_cycles(mp, 8, 1, pr8, None, 64)
+    add_step = float(acyc.mean())
+    out = {"longest_row": Lmax, "step_cycles_mean": step, "warp_steps_with_a_rounding": float((sr > 0).mean()),
+           "lane_rounding_rate": float(sr.sum() / (32.0 * L)), "add_step_cycles_mean": add_step, "sm_mhz": mhz,
+           "method": "mpres_probe_chain on the warp of the 32 longest rows (one warp alone, best of 3)"}
+    out["csr_floor_ms"] = step * Lmax / (mhz * 1e3)
+    for tpr in (4, 16):
+        out["csrv%d_floor_ms" % tpr] = (step * -(-Lmax // tpr) + np.log2(tpr) * add_step) / (mhz * 1e3)
+    out["csrv32_floor_ms"] = (float(cyc32.sum()) + 5 * add_step) / (mhz * 1e3)
+    return out
+
+
+def bench_spmv(torch, mp, stream, steps, warmup, world, hbm, mhz=None):
+    """mp_spmv_csr, mp_spmv_csrv (tpr 4, 16, 32) and mp_spmv_ell on one
+    2^20-row power-law matrix (row lengths 1..1024, mean 16), x as in the DOT,
+    8 moduli.  e2e: every step uploads the matrix (CSR forms; the 12.9 GB ELL
+    slots stay resident) and x from pinned host memory and reads y back."""
     n, m = 8, 1 << 20
+    rec = 4 * n + 40
     rng = np.random.default_rng(SEED + 2)
     irp, ja, vals = random_csr(rng, m, m, power_law_rows(rng, m))
-    mx = mp.set_d(n, doubles(rng, m, -16, 16))
+    xd = doubles(rng, m, -16, 16)
+    mx = mp.set_d(n, xd)
     x = mp.DeviceBytes.from_numpy(mx)
-    y = mp.DeviceBytes(m * mx.dtype.itemsize)
+    y = mp.DeviceBytes(m * rec)
     csr = mp.DeviceCsr(m, irp, ja, vals)
     nnz = int(irp[-1])
-    algo = nnz * 12 + (m + 1) * 4 + 2 * m * (4 * n + 40)
+    algo = nnz * 12 + (m + 1) * 4 + 2 * m * rec
+    ell = ell_on_device(torch, mp, m, irp, ja, vals)
+    algo_ell = m * ell.maxnzr * 12 + 2 * m * rec
+    p_irp, p_ja, p_vals = (pinned_copy(torch, v) for v in (irp, ja, vals))
+    p_x, p_y = pinned_copy(torch, mx), pinned_copy(torch, mx)
+    variants = [("csr", lambda: mp.spmv_csr(n, m, csr, x, y, stream=stream), "spmv_csr_kernel"),
+                ("csrv4", lambda: mp.spmv_csrv(n, m, csr, x, y, 4, stream=stream), "spmv_csrv_kernel"),
+                ("csrv16", lambda: mp.spmv_csrv(n, m, csr, x, y, 16, stream=stream), "spmv_csrv_kernel"),
+                ("csrv32", lambda: mp.spmv_csrv(n, m, csr, x, y, 32, stream=stream), "spmv_csrv_kernel"),
+                ("ell", lambda: mp.spmv_ell(n, m, ell, x, y, stream=stream), "spmv_ell_kernel")]
     out = {}
-    for name, fn in (("csr", lambda: mp.spmv_csr(n, m, csr, x, y, stream=stream)),
-                     ("csrv32", lambda: mp.spmv_csrv(n, m, csr, x, y, 32, stream=stream))):
+    ref_y = None
+    for name, fn, kern in variants:
         secs = max_over_ranks(time_steps(torch, stream, fn, steps, warmup, world), world)
         per = secs / steps
-        out[name] = {"value": world * 2 * nnz / per, "unit": "MP ops/s", "ms_per_step": per * 1e3,
-                     "launches": steps,
-                     "roofline": {"bound": "hbm", "achieved": algo / per / 1e9, "peak": hbm, "unit": "GB/s",
-                                  "frac": algo / per / 1e9 / hbm,
-                                  "traffic": traffic({"csr": "spmv_csr_kernel",
-                                                      "csrv32": "spmv_csrv_kernel"}[name])}}
+        y_res = y.t[: m * rec].clone()
+        is_ell = name == "ell"
+
+        def e2e_step(fn=fn, is_ell=is_ell):
+            if not is_ell:
+                csr.upload(p_irp, p_ja, p_vals)
+            x.t[: m * rec].copy_(torch.from_numpy(p_x.view(np.uint8).reshape(-1)), non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            fn()
+            stream.synchronize()
+            torch.from_numpy(p_y.view(np.uint8).reshape(-1)).copy_(y.t[: m * rec])
+
+        e2e_secs = e2e_time(torch, e2e_step, steps, 1, world)
+        a = algo_ell if is_ell else algo
+        h2d = m * rec + (0 if is_ell else nnz * 12 + (m + 1) * 4)
+        r = {"value": world * 2 * nnz / per, "unit": "MP ops/s", "ms_per_step": per * 1e3, "steps": steps,
+             "launches": 4 * steps,
+             "roofline": {"bound": "hbm", "achieved": a / per / 1e9, "peak": hbm, "unit": "GB/s",
+                          "frac": a / per / 1e9 / hbm, "traffic": traffic(kern) if name in ("csr", "csrv32") else None},
+             "e2e": {"value": world * 2 * nnz * steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": h2d,
+                     "d2h_bytes_per_step": m * rec,
+                     "matrix": "resident (12.9 GB of slots)" if is_ell else "uploaded every step",
+                     "result_matches_resident": bool(torch.equal(torch.from_numpy(p_y.view(np.uint8).reshape(-1)),
+                                                                 y_res.cpu()))}}
+        if is_ell:
+            r["maxnzr"] = ell.maxnzr
+            r["roofline"]["vs_csr_bytes_frac"] = algo / per / 1e9 / hbm
+            r["slots_bytes"] = m * ell.maxnzr * 12
+        if name in ("csr", "ell"):
+            if ref_y is None:
+                ref_y = y_res
+            else:
+                r["bit_identical_to_csr"] = bool(torch.equal(ref_y, y_res))
+        out[name] = r
+    ell.free()
+    del ell
+    torch.cuda.empty_cache()
+    floor = spmv_floor(mp, irp, ja, vals, mx, mhz or 2070.0)
+    for name, key in (("csr", "csr_floor_ms"), ("csrv4", "csrv4_floor_ms"), ("csrv16", "csrv16_floor_ms"),
+                      ("csrv32", "csrv32_floor_ms"), ("ell", "csr_floor_ms")):
+        out[name]["achieved_over_floor"] = out[name]["ms_per_step"] / floor[key]
     return {"workload": "mp_spmv 2^20 rows, nnz=%d (power-law 1..1024), 8 moduli" % nnz, "results": out,
-            "nnz": nnz}
+            "nnz": nnz, "chain_floor": floor, "data": (irp, ja, vals, xd, mx)}
 
 
 def device_doubles(torch, gen, count, lo, hi):
@@ -419,22 +612,25 @@ def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
         commit_s += time.perf_counter() - t0
         if w == 0:
             info = batch.info()
-            y0 = snapshot(Y)
-            plain()
-            torch.cuda.synchronize()
-            yp = snapshot(Y)
-            restore(Y, y0)
-            batch.run(stream)
-            torch.cuda.synchronize()
-            identical = same(Y, yp)
+        # both forms timed from the same y; their outputs compared on every wave
+        y0 = snapshot(Y)
         batch.run(stream)  # warm (graph upload)
+        torch.cuda.synchronize()
+        restore(Y, y0)
+        torch.cuda.synchronize()
         ev[0].record(stream)
         plain()
         ev[1].record(stream)
+        torch.cuda.synchronize()
+        yp = snapshot(Y)
+        restore(Y, y0)
+        torch.cuda.synchronize()
         ev[2].record(stream)
         batch.run(stream)
         ev[3].record(stream)
         torch.cuda.synchronize()
+        identical = identical and same(Y, yp)
+        del y0, yp
         t_plain += ev[0].elapsed_time(ev[1]) / 1e3
         t_batch += ev[2].elapsed_time(ev[3]) / 1e3
         batch.destroy()
@@ -447,7 +643,7 @@ def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
             "value": ops_total / t_batch, "unit": "MP ops/s", "plain_value": ops_total / t_plain,
             "speedup_vs_plain": t_plain / t_batch, "ms_batched": t_batch * 1e3, "ms_plain": t_plain * 1e3,
             "waves": len(waves), "wave_bytes_max": wave_bytes, "launches_batched": 2 * len(waves),
-            "launches_plain": 2 * count, "bit_identical_first_wave": identical, "shape": info,
+            "launches_plain": 2 * count, "bit_identical_all_waves": identical, "shape": info,
             "commit_s": commit_s,
             "roofline": {"bound": "hbm", "achieved": algo / t_batch / 1e9, "peak": hbm, "unit": "GB/s",
                          "frac": algo / t_batch / 1e9 / hbm, "traffic": traffic("batch_kernel", algo),
@@ -552,6 +748,15 @@ def bench_serving(torch, mp, rates=(100.0, 400.0, 1600.0), duration=1.5, budget=
             arr, snap, off, cnt = ((outs_r, mix_r, i, 1) if kinds[i] == 0 else
                                    (outs_y, mix_y, int(gy_off[i]), gemvs[int(picks[i])][0]))
             checks.append(all(torch.equal(a[sl], b[sl]) for a, b, sl in _record_slices(arr, snap, off, cnt)))
+        # SpMV requests: every request on an operand set writes the same y, so
+        # the y left by the mix must equal one plain call's
+        for p in sorted({int(picks[i]) % len(spmvs) for i in range(count) if kinds[i] == 2}):
+            m, _, csr, xa, ya = spmvs[p]
+            alone = mp.DeviceBytes(m * rec)
+            mp.spmv_csr(n, m, csr, xa, alone)
+            torch.cuda.synchronize()
+            checks.append(torch.equal(alone.t[: m * rec], ya.t[: m * rec]))
+            del alone
         del outs_r, outs_y
     return {"workload": "Poisson mix of mp_dot (n 2^10..2^22), mp_gemv (m, n 32..4096), mp_spmv_csr (rows 2^12..2^20), "
                         "8 moduli, 64 GB budget, 4 batches in flight",
@@ -567,10 +772,47 @@ def _record_slices(arr, snap, off, cnt):
 
 
 # ------------------------------------------------------------ CPU baseline --
+#
+# Every sample grows until its timed loop takes about budget_s / 2 or more, so
+# the whole default run stays within a few minutes.
 
-def cpu_gemm_sample(host, budget_s=12.0):
-    """The oracle port on a bounded sample of the GEMM: full k = 1024 chains for a
-    block of rows and columns, sized to take about budget_s seconds."""
+def _grow_blocks(run, m, budget_s, rows=8, cols=2):
+    """Runs run(rows, cols) on growing blocks of C until one takes at least
+    budget_s / 2; returns (rows, cols, seconds)."""
+    t = run(rows, cols)
+    while t < budget_s / 2 and (cols < m or rows < m):
+        if cols < m:
+            cols = min(m, cols * 2)
+        else:
+            rows = min(m, rows * 2)
+        t = run(rows, cols)
+    return rows, cols, t
+
+
+def cpu_gemm_mpfr(src, budget_s=8.0):
+    """The reference's mpfr_gemm OpenMP loop (tests/blas/v2/gemm/test_mpfr_gemm.cuh:29-60)
+    at MP_PRECISION = 480 bits on all host cores, on a block of C with the full
+    k = 1024; None where the host has no MPFR runtime."""
+    from oracle import ffi
+    L = ffi.mpfr_blas()
+    if L is None:
+        return None
+    m = 1024
+    al, be = float(src["alpha"][0]), float(src["beta"][0])
+
+    def run(rows, cols):
+        return L.gemm(rows, cols, m, al, src["A"], m, src["B"], m, be, src["C"], m, ffi.mp_precision(32))[0]
+
+    rows, cols, t = _grow_blocks(run, m, budget_s, 16, 4)
+    ops = 2.0 * rows * cols * m + 3.0 * rows * cols
+    return {"value": ops / t, "unit": "MP ops/s", "cores": L.threads(), "kind": "mpfr", "seconds": t,
+            "sample": "reference mpfr_gemm loop (MPFR, 480 bits, OpenMP) on a %dx%d block of C, k = 1024, %.1f s"
+                      % (rows, cols, t)}
+
+
+def cpu_gemm_port(host, budget_s=8.0):
+    """The oracle port (the reference's multiple-precision arithmetic restated
+    in C, OpenMP) on a bounded block of the GEMM with full k = 1024 chains."""
     from oracle import ffi
     O = ffi.oracle()
     n, m = 32, 1024
@@ -578,21 +820,14 @@ def cpu_gemm_sample(host, budget_s=12.0):
 
     # sub-problem: C(0:rows, 0:cols) = alpha * A(0:rows, :) * B(:, 0:cols) + beta * C(0:rows, 0:cols),
     # passed with the full leading dimensions so no copy is needed
-    def time_block(rows, cols):
+    def run(rows, cols):
         t0 = time.perf_counter()
         O.gemm(n, rows, cols, m, host["alpha"], A, m, B, m, host["beta"], C[: m * cols], m)
         return time.perf_counter() - t0
 
-    rows, cols = 8, 2
-    t = time_block(rows, cols)
-    while t < budget_s / 2 and (cols < m or rows < m):
-        if cols < m:
-            cols = min(m, cols * 2)
-        else:
-            rows = min(m, rows * 2)
-        t = time_block(rows, cols)
+    rows, cols, t = _grow_blocks(run, m, budget_s)
     ops = 2.0 * rows * cols * m + 3.0 * rows * cols
-    return {"value": ops / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
+    return {"value": ops / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port", "seconds": t,
             "sample": "oracle mp_gemm on a %dx%d block of C (k = 1024, 32 moduli), %.1f s" % (rows, cols, t)}
 
 
@@ -622,7 +857,7 @@ def cpu_gemv_sample(torch, mp, budget_s=6.0):
             "sample": "oracle mp_gemv on the first %d of the 4096 instances, %.1f s" % (done, t)}
 
 
-def cpu_dot_sample(mx, my, budget_s=6.0):
+def cpu_dot_port(mx, my, budget_s=6.0):
     from oracle import ffi
     O = ffi.oracle()
     count = 1 << 16
@@ -636,7 +871,100 @@ def cpu_dot_sample(mx, my, budget_s=6.0):
             "sample": "oracle mp_dot on the first 2^16 elements, %d runs in %.1f s" % (reps, t)}
 
 
+def cpu_dot_mpfr(xd, yd, budget_s=6.0):
+    """The reference's mpfr_dot OpenMP loop (tests/blas/performance/test_dot_performance.cu:152-174)
+    at 120 bits over the whole n = 2^20, repeated until budget_s of loop time."""
+    from oracle import ffi
+    L = ffi.mpfr_blas()
+    if L is None:
+        return None
+    t = 0.0
+    reps = 0
+    w0 = time.perf_counter()
+    while (t < budget_s and time.perf_counter() - w0 < 3 * budget_s) or reps == 0:
+        t += L.dot(xd, yd, ffi.mp_precision(8))[0]
+        reps += 1
+    return {"value": 2.0 * len(xd) * reps / t, "unit": "MP ops/s", "cores": L.threads(), "kind": "mpfr",
+            "sample": "reference mpfr_dot loop (MPFR, 120 bits, OpenMP), n = 2^20, %d runs, %.1f s" % (reps, t)}
+
+
+def _row_block(irp, rows):
+    return irp[: rows + 1], int(irp[rows])
+
+
+def cpu_spmv_mpfr(irp, ja, vals, xd, budget_s=6.0):
+    """The reference's mpfr_mpspmv_csr OpenMP loop (tests/sparse/spmv/csr/test_mpfr_spmv_csr.cuh:33-51)
+    at 120 bits on the first rows of the benchmark matrix."""
+    from oracle import ffi
+    L = ffi.mpfr_blas()
+    if L is None:
+        return None
+    m = len(irp) - 1
+    rows = 4096
+    while True:
+        sub, nnz = _row_block(irp, rows)
+        t = L.spmv_csr(rows, sub, ja, vals, xd, ffi.mp_precision(8))[0]
+        if t >= budget_s / 2 or rows >= m:
+            break
+        rows = min(m, rows * 2)
+    return {"value": 2.0 * nnz / t, "unit": "MP ops/s", "cores": L.threads(), "kind": "mpfr",
+            "sample": "reference mpfr_mpspmv_csr loop (MPFR, 120 bits, OpenMP) on the first %d rows (%d nnz), %.1f s"
+                      % (rows, nnz, t)}
+
+
+def cpu_spmv_port(irp, ja, vals, mx, budget_s=6.0):
+    """The oracle port of mp_spmv_csr on the first rows of the benchmark matrix."""
+    from oracle import ffi
+    O = ffi.oracle()
+    m = len(irp) - 1
+    rows = 4096
+    while True:
+        sub, nnz = _row_block(irp, rows)
+        t0 = time.perf_counter()
+        O.spmv_csr(8, rows, sub, ja, vals, mx)
+        t = time.perf_counter() - t0
+        if t >= budget_s / 2 or rows >= m:
+            break
+        rows = min(m, rows * 2)
+    return {"value": 2.0 * nnz / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
+            "sample": "oracle mp_spmv_csr on the first %d rows (%d nnz), %.1f s" % (rows, nnz, t)}
+
+
 # -------------------------------------------------------------------- main --
+
+def reference_arm(args, world):
+    """The reference's CPU path for the headline GEMM on this host's cores: the
+    MPFR mpfr_gemm loop (the port where the host has no MPFR runtime), one
+    bounded block of C per step.  Loads only oracle/ libraries."""
+    from oracle import ffi
+    ffi.build_oracle()
+    src = gemm_doubles()
+    budget = min(8.0, max(2.0, 150.0 / max(1, args.steps)))
+    if ffi.mpfr_blas() is not None:
+        def sample(b):
+            return cpu_gemm_mpfr(src, b)
+    else:
+        host = {k: ffi.oracle().set_d(32, v) for k, v in src.items()}
+
+        def sample(b):
+            return cpu_gemm_port(host, b)
+    for _ in range(args.warmup):
+        sample(1.0)
+    samples = [sample(budget) for _ in range(args.steps)]
+    v = statistics.median(s["value"] for s in samples)
+    cb = dict(samples[0])
+    cb["value"] = v
+    secs = [s["seconds"] for s in samples]
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "MP ops/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(secs) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "MPFR 480-bit (reference CPU path)" if cb["kind"] == "mpfr" else "int32 residues + f64 interval bounds",
+        "data": "synthetic (seeded u*2^e entries; the reference publishes no dataset)",
+        "config": gemm_config(world),
+        "cpu_baseline": cb, "e2e": {"value": v, "unit": "MP ops/s", "h2d_bytes_per_step": 0,
+                                    "d2h_bytes_per_step": 0}}))
+
 
 def main():
     ap = argparse.ArgumentParser()
@@ -646,32 +974,13 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extra", action="store_true", help="headline GEMM only")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-GEMV and serving workloads")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
     args = ap.parse_args()
     world, rank, local = dist()
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        import mpres_gb300 as mp
-        import build
-        build.build()
-        host = gemm_inputs(mp)
-        samples = []
-        for _ in range(args.warmup):
-            cpu_gemm_sample(host, budget_s=2.0)
-        for _ in range(args.steps):
-            samples.append(cpu_gemm_sample(host, budget_s=8.0))
-        v = statistics.median(s["value"] for s in samples)
-        cb = dict(samples[0])
-        cb["value"] = v
-        print(json.dumps({
-            "impl": "reference", "metric": METRIC, "value": v, "unit": "MP ops/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int32 residues + f64 interval bounds",
-            "data": "synthetic (seeded)",
-            "config": gemm_config(world),
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": "MP ops/s", "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}))
+        if rank == 0:
+            reference_arm(args, world)
         return
 
     import torch
@@ -692,10 +1001,11 @@ def main():
     g = bench_gemm(torch, mp, stream, args.steps, max(3, args.warmup), world, rank, local)
     extra = {}
     if not args.no_extra:
-        dot = bench_dot(torch, mp, stream, 20, 3, world, hbm)
-        spmv = bench_spmv(torch, mp, stream, 5, 2, world, hbm)
+        mhz = g["clocks"].get("sm_mhz") or 2070.0
+        dot = bench_dot(torch, mp, stream, 20, 3, world, hbm, mhz)
+        spmv = bench_spmv(torch, mp, stream, 5, 3, world, hbm, mhz)
         extra["mp_dot"] = {k: v for k, v in dot.items() if k != "data"}
-        extra["mp_spmv"] = spmv
+        extra["mp_spmv"] = {k: v for k, v in spmv.items() if k != "data"}
         if not args.no_batch:
             extra["batched_gemv"] = bench_batched_gemv(torch, mp, stream, hbm)
             extra["serving"] = bench_serving(torch, mp)
@@ -704,18 +1014,25 @@ def main():
         "warmup": max(3, args.warmup), "ms_per_step": g["secs"] / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32 residues + f64 interval bounds",
         "data": "synthetic (seeded u*2^e entries; the reference publishes no dataset)",
-        "config": dict(gemm_config(world), l2="inputs larger than L2 (3 x 176 MB)",
-                       c_per_step="C restored from its initial value by a device copy inside each timed step"),
+        "config": gemm_config(world),
         "roofline": g["roofline"], "hbm_peak_source": peak_src, "e2e": g["e2e"], "clocks": g["clocks"],
         "gpu_launches": g["launches"],
     }
     line.update(extra)
-    if rank == 0:
-        line["cpu_baseline"] = cpu_gemm_sample(g["host"])
+    if rank == 0 and not args.no_cpu:
+        mp_cb, port_cb = cpu_gemm_mpfr(g["src"]), cpu_gemm_port(g["host"])
+        line["cpu_baseline"] = mp_cb or port_cb
+        line["cpu_baseline_port"] = port_cb
         if not args.no_extra:
-            line["mp_dot"]["cpu_baseline"] = cpu_dot_sample(*dot["data"])
+            xd, yd, mx, my = dot["data"]
+            line["mp_dot"]["cpu_baseline"] = cpu_dot_mpfr(xd, yd) or cpu_dot_port(mx, my)
+            line["mp_dot"]["cpu_baseline_port"] = cpu_dot_port(mx, my)
+            irp, ja, vals, sxd, smx = spmv["data"]
+            line["mp_spmv"]["cpu_baseline"] = cpu_spmv_mpfr(irp, ja, vals, sxd) or cpu_spmv_port(irp, ja, vals, smx)
+            line["mp_spmv"]["cpu_baseline_port"] = cpu_spmv_port(irp, ja, vals, smx)
             if "batched_gemv" in line:
                 line["batched_gemv"]["cpu_baseline"] = cpu_gemv_sample(torch, mp)
+    if rank == 0:
         print(json.dumps(line))
     if world > 1:
         import torch.distributed as td

@@ -42,6 +42,18 @@ int mpres_probe_ceil_log2(const double *x, double *out, size_t count, void *stre
  * All pointers are device memory. */
 int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *out, size_t count, void *stream);
 
+/* Latency of the reduction chains on one warp running alone: 32 chains of len
+ * steps, lane l over elements l*len .. l*len+len-1 of
+ *   kind 0: acc = acc + x[i]*y[i]   (cuda::mp_mul + cuda::mp_add, the DOT/GEMV step)
+ *   kind 1: acc = acc + x[i]        (cuda::mp_add alone)
+ *   kind 2: acc = acc + x[i]*y[i]   (cuda::mp_mul_d + cuda::mp_add, the SpMV step; y = double[])
+ * x, y: AoS mp_float_t[32*len] (y double[32*len] for kind 2); cycles: long long[len]
+ * receives the SM cycles of each step; rounds: unsigned[len] the number of lanes
+ * whose product (bits 0-7) and sum (bits 8-15) rounded at that step; result:
+ * mp_float_t[32], each lane's sum.  All pointers are device memory. */
+int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
+                      unsigned *rounds, void *result, void *stream);
+
 /* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
  * element per thread: the device functions the BLAS kernels are built from,
  * exposed so that each can be checked against the reference on its own.

@@ -201,26 +201,38 @@ int require(int nmod) {
 }
 
 /* Workspace of (device, stream), grown on demand: the first call on a stream
- * (or a call needing more room than before) allocates; later calls do not. */
-int workspace(cudaStream_t s, size_t bytes, Workspace &out) {
+ * (or a call needing more room than before) allocates; later calls do not.
+ * The larger buffer is allocated before the old one is released, so a request
+ * that cannot be met leaves the stream's existing workspace in place (and the
+ * next smaller call does not allocate again).  On failure nothing is reported
+ * here: the caller decides whether the call fails (status_cuda) or takes a
+ * path without scratch. */
+cudaError_t workspace_grow(cudaStream_t s, size_t bytes, Workspace &out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lk(g_mu);
     Workspace &w = g_ws[WsKey{dev, s}];
     if (w.bytes < bytes) {
-        if (w.ptr) {
-            cudaStreamSynchronize(s);
-            cudaFree(w.ptr);
-            w.ptr = nullptr;
-            w.bytes = 0;
+        const size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
+        void *p = nullptr;
+        if ((e = cudaMalloc(&p, want)) != cudaSuccess) {
+            cudaGetLastError(); /* the failed allocation is not a sticky error */
+            return e;
         }
-        size_t want = bytes < (1u << 20) ? (1u << 20) : bytes;
-        if ((e = cudaMalloc(&w.ptr, want)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(workspace)");
+        if (w.ptr) {
+            cudaStreamSynchronize(s); /* work queued on s may still use the old buffer */
+            cudaFree(w.ptr);
+        }
+        w.ptr = p;
         w.bytes = want;
     }
     out = w;
-    return MPRES_SUCCESS;
+    return cudaSuccess;
+}
+int workspace(cudaStream_t s, size_t bytes, Workspace &out) {
+    const cudaError_t e = workspace_grow(s, bytes, out);
+    return e == cudaSuccess ? MPRES_SUCCESS : cuda_fail(e, "cudaMalloc(workspace)");
 }
 
 size_t mp_size(int nmod) { return 4 * (size_t)nmod + 40; }
@@ -690,10 +702,8 @@ int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_a
      * the workspace cannot grow (same bits, no scratch) */
     const char *no_scratch = std::getenv("MPRES_GEMM_NO_SCRATCH");
     const bool scratch = !(no_scratch && no_scratch[0] == '1');
-    if (scratch && workspace(s, gemm_workspace_bytes(nmod, m, n, k), ws) != MPRES_SUCCESS) {
+    if (scratch && workspace_grow(s, gemm_workspace_bytes(nmod, m, n, k), ws) != cudaSuccess)
         ws = Workspace{}; /* no room for W(A), W(B): the step-by-step chain, no scratch */
-        cudaGetLastError(); /* the failed allocation is not this call's error */
-    }
     cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemm");
 }
@@ -755,6 +765,15 @@ int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *o
     if (!a || !out || (which == 1 && !b)) return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_check: null pointer");
     cudaError_t e = launch_check(which, nmod, a, b, out, (long long)count, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_check");
+}
+
+int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
+                      unsigned *rounds, void *result, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (kind < 0 || kind > 2 || len <= 0 || !x || (kind != 1 && !y) || !cycles || !rounds || !result)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_chain: bad arguments");
+    cudaError_t e = launch_chain_probe(nmod, kind, x, y, len, cycles, rounds, result, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_chain");
 }
 
 int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {

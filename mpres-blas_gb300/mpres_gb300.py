@@ -106,6 +106,7 @@ _SIGS = {
     "mpres_elementwise": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_ceil_log2": (I, [P, P, SZ, P]),
     "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
+    "mpres_probe_chain": (I, [I, I, P, P, I, P, P, P, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
     "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
 }
@@ -450,6 +451,17 @@ class DeviceCsr:
               "mpres_csr_host2device")
         self._live = True
 
+    def upload(self, irp, ja, vals):
+        """Copies host arrays of the same shape into this matrix (csr_host2device);
+        contiguous int32 / int32 / float64 arrays, e.g. in pinned memory, are used in place."""
+        irp = np.ascontiguousarray(irp, dtype=np.int32)
+        ja = np.ascontiguousarray(ja, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float64)
+        assert len(irp) == self.m + 1 and len(ja) == self.nnz and len(vals) == self.nnz
+        host = CsrT(vals.ctypes.data, ja.ctypes.data, irp.ctypes.data)
+        check(lib().mpres_csr_host2device(ctypes.byref(self.c), ctypes.byref(host), self.m, self.nnz),
+              "mpres_csr_host2device")
+
     def free(self):
         if self._live:
             check(lib().mpres_csr_clear(ctypes.byref(self.c)), "mpres_csr_clear")
@@ -468,10 +480,23 @@ class DeviceEll:
               "mpres_ell_host2device")
         self._live = True
 
+    @classmethod
+    def from_tensors(cls, m, maxnzr, ja, vals):
+        """An ell_t over CUDA tensors (int32 ja, float64 vals, maxnzr * m slots
+        each, column-major) that torch owns; free() only drops the references."""
+        assert ja.numel() == vals.numel() == m * maxnzr
+        self = cls.__new__(cls)
+        self.m, self.maxnzr = m, maxnzr
+        self._tensors = (ja, vals)
+        self.e = EllT(vals.data_ptr(), ja.data_ptr())
+        self._live = False
+        return self
+
     def free(self):
         if self._live:
             check(lib().mpres_ell_clear(ctypes.byref(self.e)), "mpres_ell_clear")
             self._live = False
+        self._tensors = None
 
 
 def dot(nmod, n, x, y, r, incx=1, incy=1, order=(512, 128, 8192, 256, 64), buffer=None, stream=None):
@@ -675,6 +700,28 @@ def probe_ceil_log2(x):
     check(lib().mpres_probe_ceil_log2(dx.ptr, do.ptr, x.size, None), "mpres_probe_ceil_log2")
     torch.cuda.synchronize()
     return do.to_numpy(np.float64, x.size)
+
+
+PROBE_MUL_ADD, PROBE_ADD, PROBE_MULD_ADD = 0, 1, 2
+
+
+def probe_chain(nmod, kind, x, y, length):
+    """One warp's reduction chains (mpres_probe_chain): x, y host arrays of
+    32*length records (y doubles for PROBE_MULD_ADD, unused for PROBE_ADD).
+    Returns (cycles per step, lanes whose product rounded, lanes whose sum
+    rounded, the 32 chains' sums)."""
+    import torch
+    x = np.ascontiguousarray(x)
+    assert len(x) == 32 * length
+    dx = DeviceBytes.from_numpy(x)
+    dy = DeviceBytes.from_numpy(np.ascontiguousarray(y)) if y is not None else None
+    cyc, rnd, res = DeviceBytes(8 * length), DeviceBytes(4 * length), DeviceBytes(32 * x.dtype.itemsize)
+    check(lib().mpres_probe_chain(nmod, kind, dx.ptr, dy.ptr if dy else None, length, cyc.ptr, rnd.ptr, res.ptr,
+                                  None), "mpres_probe_chain")
+    torch.cuda.synchronize()
+    r = rnd.to_numpy(np.uint32, length)
+    return (cyc.to_numpy(np.int64, length), (r & 0xff).astype(np.int64), ((r >> 8) & 0xff).astype(np.int64),
+            res.to_numpy(x.dtype, 32))
 
 
 def probe_check(which, nmod, a, b=None):

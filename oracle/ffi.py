@@ -37,7 +37,72 @@ def build_oracle():
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
 
 
+def reference_root():
+    """The reference checkout's root directory, or None where it is absent (the
+    location is named by the recipe oracle/ref/build_ref.sh alone)."""
+    r = subprocess.run(["bash", str(HERE / "ref" / "build_ref.sh"), "--where"], capture_output=True, text=True)
+    root = r.stdout.strip()
+    return pathlib.Path(root) if r.returncode == 0 and root else None
+
+
 _oracle = None
+_mpfr = None
+MPFR_SO = HERE / "_build" / "libmpres_mpfr.so"
+
+
+class MpfrBlas:
+    """The reference's MPFR/OpenMP loops (oracle/mpfr_blas.c).  Each call
+    returns (seconds of the timed loop, results rounded to double)."""
+
+    D = ctypes.POINTER(ctypes.c_double)
+
+    def __init__(self, lib):
+        self.lib = lib
+        for name in ("mpb_dot", "mpb_gemm", "mpb_spmv_csr"):
+            getattr(lib, name).restype = ctypes.c_double
+
+    def threads(self):
+        return int(self.lib.mpb_max_threads())
+
+    def dot(self, x, y, prec, threads=None):
+        x, y = np.ascontiguousarray(x, np.float64), np.ascontiguousarray(y, np.float64)
+        out = np.zeros(1)
+        t = self.lib.mpb_dot(len(x), ptr(x), ptr(y), ctypes.c_long(prec), threads or self.threads(), ptr(out))
+        return t, out[0]
+
+    def gemm(self, rows, cols, k, alpha, A, lda, B, ldb, beta, C, ldc, prec, threads=None):
+        A, B, C = (np.ascontiguousarray(v, np.float64) for v in (A, B, C))
+        out = np.zeros(rows * cols)
+        t = self.lib.mpb_gemm(rows, cols, k, ctypes.c_double(alpha), ptr(A), lda, ptr(B), ldb, ctypes.c_double(beta),
+                              ptr(C), ldc, ctypes.c_long(prec), threads or self.threads(), ptr(out))
+        if t < 0:
+            raise MemoryError("mpb_gemm: allocation failed")
+        return t, out
+
+    def spmv_csr(self, m, irp, ja, vals, x, prec, threads=None):
+        irp, ja = np.ascontiguousarray(irp, np.int32), np.ascontiguousarray(ja, np.int32)
+        vals, x = np.ascontiguousarray(vals, np.float64), np.ascontiguousarray(x, np.float64)
+        out = np.zeros(m)
+        t = self.lib.mpb_spmv_csr(m, len(x), ptr(irp), ptr(ja), ptr(vals), ptr(x), ctypes.c_long(prec),
+                                  threads or self.threads(), ptr(out))
+        return t, out
+
+
+def mpfr_blas():
+    """The MPFR baseline library, or None where the host has no libmpfr.so.6."""
+    global _mpfr
+    if _mpfr is None:
+        if not MPFR_SO.exists():
+            build_oracle()
+        if not MPFR_SO.exists():
+            return None
+        _mpfr = MpfrBlas(ctypes.CDLL(str(MPFR_SO)))
+    return _mpfr
+
+
+def mp_precision(n):
+    """MP_PRECISION of the predefined set of n moduli (src/arith/arith_utils.cuh:50)."""
+    return {8: 120, 16: 240, 32: 480}[n]
 
 
 def oracle():

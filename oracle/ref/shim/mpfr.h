@@ -4,7 +4,8 @@
  * MPFR manual: the mpfr_t layout, the rounding-mode enumeration and the
  * documented functions the reference's constant set-up and conversions call.
  *
- * Test infrastructure only (oracle/_ref/ build), never used by the product.
+ * Test infrastructure only (the oracle/_ref/ build and the MPFR baseline
+ * oracle/mpfr_blas.c), never used by the product.
  */
 #ifndef ORACLE_SHIM_MPFR_H
 #define ORACLE_SHIM_MPFR_H
@@ -51,6 +52,7 @@ int mpfr_set_str(mpfr_ptr, const char *, int, mpfr_rnd_t);
 int mpfr_add(mpfr_ptr, mpfr_srcptr, mpfr_srcptr, mpfr_rnd_t);
 int mpfr_sub(mpfr_ptr, mpfr_srcptr, mpfr_srcptr, mpfr_rnd_t);
 int mpfr_mul(mpfr_ptr, mpfr_srcptr, mpfr_srcptr, mpfr_rnd_t);
+int mpfr_mul_d(mpfr_ptr, mpfr_srcptr, double, mpfr_rnd_t);
 int mpfr_div(mpfr_ptr, mpfr_srcptr, mpfr_srcptr, mpfr_rnd_t);
 int mpfr_sqrt(mpfr_ptr, mpfr_srcptr, mpfr_rnd_t);
 int mpfr_log2(mpfr_ptr, mpfr_srcptr, mpfr_rnd_t);

@@ -150,3 +150,31 @@ def test_ceil_log2_of_doubles_matches_cuda(gpu):
     out = gpu.probe_check(3, 8, allx)
     bad = np.nonzero(out[:, 0] != out[:, 1])[0]
     assert len(bad) == 0, [(float.hex(float(allx[i])), out[i].tolist()) for i in bad[:5]]
+
+
+@pytest.mark.parametrize("n,kind", [(8, 0), (8, 1), (8, 2), (16, 0), (32, 2)])
+def test_chain_probe_computes_the_chains(gpu, oracle, n, kind):
+    """The latency probe runs the real reduction step: each lane's chain sum
+    equals the oracle's sequential chain, and it reports at least one cycle
+    per step and round counts no larger than the warp."""
+    rng = np.random.default_rng(helpers.SEED + 950 + n + kind)
+    length = 40
+    x = gpu.set_d(n, helpers.doubles(rng, 32 * length, -16, 16))
+    y = (helpers.doubles(rng, 32 * length, -8, 8) if kind == 2
+         else gpu.set_d(n, helpers.doubles(rng, 32 * length, -16, 16)) if kind == 0 else None)
+    cycles, prod_rounds, sum_rounds, res = gpu.probe_chain(n, kind, x, y, length)
+    acc = np.zeros(32, x.dtype)
+    acc["eval"]["frac"] = 0.0
+    for t in range(length):
+        idx = np.arange(32) * length + t
+        a = x[idx].copy()
+        if kind == 0:
+            p = oracle.mul(n, a, y[idx].copy())
+        elif kind == 2:
+            p = oracle.mul_d(n, a, np.ascontiguousarray(y[idx]))
+        else:
+            p = a
+        acc = oracle.add(n, acc, p)
+    eq(res, acc)
+    assert (cycles > 0).all()
+    assert (prod_rounds <= 32).all() and (sum_rounds <= 32).all()

@@ -261,10 +261,9 @@ def test_gemm_transposed_is_not_supported(gpu):
         gpu.gemm(8, 2, 2, 2, a, d, 2, d, 2, a, d, 2, transa=gpu.TRANS)
 
 
-def test_gemm_full_size_sampled(gpu, oracle):
-    """m = n = k = 1024 with 32 moduli (the GEMM benchmark): entries checked
-    bit-for-bit against the oracle on a sample of 24 outputs (each one is a
-    1024-long chain, computed by the oracle on the row/column it depends on)."""
+def test_gemm_full_size(gpu, oracle):
+    """m = n = k = 1024 with 32 moduli, the GEMM benchmark's inputs: all
+    1 048 576 outputs bit-for-bit against the oracle (each a 1024-long k chain)."""
     n, m = 32, 1024
     rng = np.random.default_rng(helpers.SEED + 1)
     A = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
@@ -272,13 +271,7 @@ def test_gemm_full_size_sampled(gpu, oracle):
     C = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
     al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
     r = run_gemm(gpu, n, m, m, m, al, A, m, B, m, be, C, m)
-    for _ in range(24):
-        row, col = (int(v) for v in rng.integers(0, m, 2))
-        arow = np.ascontiguousarray(A[row::m])  # A(row, :) with stride lda = m
-        bcol = np.ascontiguousarray(B[col * m:(col + 1) * m])
-        c = C[row + col * m:row + col * m + 1].copy()
-        want = oracle.gemm(n, 1, 1, m, al, arow, 1, bcol, m, be, c, 1)
-        eq(r[row + col * m:row + col * m + 1], want)
+    eq(r, oracle.gemm(n, m, m, m, al, A, m, B, m, be, C, m))
 
 
 # ----------------------------------------------------------------- SpMV ----
@@ -325,15 +318,70 @@ def test_spmv_random_vs_oracle(gpu, oracle, n):
        oracle.spmv_ell(n, small, maxnzr, eja, eas, mx))
 
 
-def test_spmv_full_size(gpu, oracle):
-    """2^20 rows, power-law row lengths 1..1024 (mean 16): the SpMV benchmark, all
-    outputs bit-identical to the oracle for CSR and CSR-vector with 32 lanes."""
+@pytest.fixture(scope="module")
+def spmv_bench_matrix(gpu, oracle):
+    """The SpMV benchmark's inputs: 2^20 rows, power-law row lengths 1..1024
+    (mean 16), 8 moduli; with the oracle's CSR result over every row."""
     rng = np.random.default_rng(helpers.SEED + 2)
     m = 1 << 20
     irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
     mx = gpu.set_d(8, helpers.doubles(rng, m, -16, 16))
-    eq(run_spmv(gpu, 8, "csr", m, mx, irp, ja, vals), oracle.spmv_csr(8, m, irp, ja, vals, mx))
-    eq(run_spmv(gpu, 8, "csrv", m, mx, irp, ja, vals, tpr=32), oracle.spmv_csrv(8, m, 32, irp, ja, vals, mx))
+    return m, irp, ja, vals, mx, oracle.spmv_csr(8, m, irp, ja, vals, mx)
+
+
+def test_spmv_full_size_csr(gpu, spmv_bench_matrix):
+    m, irp, ja, vals, mx, want = spmv_bench_matrix
+    eq(run_spmv(gpu, 8, "csr", m, mx, irp, ja, vals), want)
+
+
+@pytest.mark.parametrize("tpr", [4, 16, 32])
+def test_spmv_full_size_csrv(gpu, oracle, spmv_bench_matrix, tpr):
+    """CSR-vector at the tpr values of the reference's SpMV driver
+    (tests/sparse/test_spmv.cu:179-181), every row against the oracle."""
+    m, irp, ja, vals, mx, _ = spmv_bench_matrix
+    eq(run_spmv(gpu, 8, "csrv", m, mx, irp, ja, vals, tpr=tpr), oracle.spmv_csrv(8, m, tpr, irp, ja, vals, mx))
+
+
+def test_spmv_full_size_ell(gpu, oracle, spmv_bench_matrix):
+    """ELLPACK of the benchmark matrix (maxnzr slots per row, about 12.9 GB,
+    built on the device): every row equals the CSR chain (ELL keeps a row's entry
+    order and skips only stored zeros, and the values are never zero), which
+    equals the oracle; a row sample holding every row of the longest bucket and
+    rows of every length is also checked against the oracle's own ELL."""
+    import torch
+    m, irp, ja, vals, mx, want = spmv_bench_matrix
+    lens = np.diff(irp).astype(np.int64)
+    maxnzr = int(lens.max())
+    irp_t = torch.from_numpy(irp.astype(np.int64)).cuda()
+    rows = torch.repeat_interleave(torch.arange(m, device="cuda"), torch.from_numpy(lens).cuda())
+    slot = (torch.arange(len(ja), device="cuda") - irp_t[:-1][rows]) * m + rows
+    del rows
+    ell_ja = torch.zeros(maxnzr * m, dtype=torch.int32, device="cuda")
+    ell_as = torch.zeros(maxnzr * m, dtype=torch.float64, device="cuda")
+    ell_ja[slot] = torch.from_numpy(ja).cuda()
+    ell_as[slot] = torch.from_numpy(vals).cuda()
+    del slot
+    e = gpu.DeviceEll.from_tensors(m, maxnzr, ell_ja, ell_as)
+    x = gpu.DeviceBytes.from_numpy(mx)
+    y = gpu.DeviceBytes(m * mx.dtype.itemsize)
+    gpu.spmv_ell(8, m, e, x, y)
+    sync()
+    got = y.to_numpy(mx.dtype, m)
+    e.free()
+    del ell_ja, ell_as
+    torch.cuda.empty_cache()
+    eq(got, want)
+    rng = np.random.default_rng(helpers.SEED + 23)
+    sample = set(np.flatnonzero(lens >= maxnzr // 2).tolist())
+    for L in np.unique(lens):
+        cand = np.flatnonzero(lens == L)
+        sample.update(rng.choice(cand, min(3, len(cand)), replace=False).tolist())
+    sample = np.array(sorted(sample))
+    sirp = np.concatenate([[0], np.cumsum(lens[sample])]).astype(np.int32)
+    sja = np.concatenate([ja[irp[r]:irp[r + 1]] for r in sample])
+    svals = np.concatenate([vals[irp[r]:irp[r + 1]] for r in sample])
+    smax, eja, eas = helpers.csr_to_ell(len(sample), sirp, sja, svals)
+    eq(got[sample], oracle.spmv_ell(8, len(sample), smax, eja, eas, mx))
 
 
 # ---------------------------------------------------------------- errors ----
