@@ -335,7 +335,8 @@ def dot_floor(mp, mx, my, count, g3, b3, mhz):
         ok = idx < count
         idx = np.where(ok, idx, 0)
         cyc, pr, sr = chain_cycles(mp, 8, 0, mx[idx], my[idx], steps)
-        chain.append((int(cyc.sum()), float((sr > 0).mean()), float(sr.sum() / (32.0 * steps))))
+        fcyc, _, _ = chain_cycles(mp, 8, 0 + mp.PROBE_FIXED_POINT, mx[idx], my[idx], steps)
+        chain.append((int(cyc.sum()), float((sr > 0).mean()), float(sr.sum() / (32.0 * steps)), int(fcyc.sum())))
     # additions of partial sums: products summed pairwise, as the trees do
     pr8 = mp.elementwise(8, mp.OP_MUL, mx[: 32 * 64], my[: 32 * 64])
     acyc, _, asr = chain_cycles(mp, 8, 1, pr8, None, 64)
@@ -347,6 +348,7 @@ def dot_floor(mp, mx, my, count, g3, b3, mhz):
     return {"floor_ms": cycles / (mhz * 1e3), "chain_cycles_worst_warp": worst, "steps": steps,
             "step_cycles_mean": worst / steps, "add_step_cycles_mean": add_step,
             "warp_steps_with_a_rounding": max(c[1] for c in chain), "lane_rounding_rate": chain[0][2],
+            "step_cycles_mean_fixed_point_eval": max(c[3] for c in chain) / steps,
             "sm_mhz": mhz, "method": "mpres_probe_chain: one warp alone, clock64 per step, best of 3; "
                                      "chain of the longest of 4 sampled warps + 2*log2(b3) + g3/b3 add steps"}
 
@@ -422,6 +424,7 @@ def spmv_floor(mp, irp, ja, vals, mx, mhz):
     idx = np.concatenate([np.arange(irp[r], irp[r] + L) for r in order])
     cyc, _, sr = chain_cycles(mp, 8, 2, mx[ja[idx]], vals[idx], L)
     step = float(cyc.mean())
+    fcyc, _, _ = chain_cycles(mp, 8, 2 + mp.PROBE_FIXED_POINT, mx[ja[idx]], vals[idx], L)
     r0 = int(order[0])
     sub = -(-Lmax // 32)
     lane_idx = np.array([[irp[r0] + l + 32 * t if l + 32 * t < Lmax else irp[r0] + l for t in range(sub)]
@@ -430,7 +433,8 @@ def spmv_floor(mp, irp, ja, vals, mx, mhz):
     pr8 = mp.elementwise(8, mp.OP_MUL, mx[: 32 * 64], mx[32 * 64: 64 * 64])
     acyc, _, _ = chain_cycles(mp, 8, 1, pr8, None, 64)
     add_step = float(acyc.mean())
-    out = {"longest_row": Lmax, "step_cycles_mean": step, "warp_steps_with_a_rounding": float((sr > 0).mean()),
+    out = {"longest_row": Lmax, "step_cycles_mean": step, "step_cycles_mean_fixed_point_eval": float(fcyc.mean()),
+           "warp_steps_with_a_rounding": float((sr > 0).mean()),
            "lane_rounding_rate": float(sr.sum() / (32.0 * L)), "add_step_cycles_mean": add_step, "sm_mhz": mhz,
            "method": "mpres_probe_chain on the warp of the 32 longest rows (one warp alone, best of 3)"}
     out["csr_floor_ms"] = step * Lmax / (mhz * 1e3)

@@ -50,7 +50,10 @@ int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *o
  * x, y: AoS mp_float_t[32*len] (y double[32*len] for kind 2); cycles: long long[len]
  * receives the SM cycles of each step; rounds: unsigned[len] the number of lanes
  * whose product (bits 0-7) and sum (bits 8-15) rounded at that step; result:
- * mp_float_t[32], each lane's sum.  All pointers are device memory. */
+ * mp_float_t[32], each lane's sum.  All pointers are device memory.
+ * kind + MPRES_PROBE_FIXED_POINT runs the same chains with the interval
+ * evaluation in fixed point on the integer pipes instead of FP64 (same bits). */
+#define MPRES_PROBE_FIXED_POINT 16
 int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                       unsigned *rounds, void *result, void *stream);
 

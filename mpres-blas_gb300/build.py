@@ -19,7 +19,7 @@ LIB = OUT / "libmpres_gb300.so"
 INCLUDE = HERE.parent / "include"
 
 CU_SOURCES = ["dot.cu", "gemv.cu", "gemm.cu", "spmv.cu", "capi.cu", "probe.cu", "elementwise.cu", "convert.cu",
-              "batch.cu", "solver.cu"]
+              "batch.cu", "solver.cu", "probe_fx.cu"]
 CPP_SOURCES = ["host_tables.cpp", "host_convert.cpp", "host_mpfr.cpp", "server.cpp", "mtx.cpp"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

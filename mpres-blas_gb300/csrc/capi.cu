@@ -136,6 +136,7 @@ cudaError_t upload_all(const HostTables &h, const int *dpow2, const int *dpow2_i
     if ((e = upload_tables_convert(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_batch(N, &t)) != cudaSuccess) return e;
     if ((e = upload_tables_solver(N, &t)) != cudaSuccess) return e;
+    if ((e = upload_tables_probe_fx(N, &t)) != cudaSuccess) return e;
     return upload_tables_spmv(N, &t);
 }
 
@@ -770,9 +771,13 @@ int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *o
 int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                       unsigned *rounds, void *result, void *stream) {
     if (int st = require(nmod)) return st;
-    if (kind < 0 || kind > 2 || len <= 0 || !x || (kind != 1 && !y) || !cycles || !rounds || !result)
+    const int k = kind & 0xf, fixed = kind >> 4;
+    if (k < 0 || k > 2 || fixed < 0 || fixed > 1 || len <= 0 || !x || (k != 1 && !y) || !cycles || !rounds ||
+        !result)
         return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_chain: bad arguments");
-    cudaError_t e = launch_chain_probe(nmod, kind, x, y, len, cycles, rounds, result, static_cast<cudaStream_t>(stream));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = fixed ? launch_chain_probe_fx(nmod, k, x, y, len, cycles, rounds, result, s)
+                          : launch_chain_probe_fp64(nmod, k, x, y, len, cycles, rounds, result, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_chain");
 }
 

@@ -29,6 +29,7 @@ cudaError_t upload_tables_elementwise(int n, const void *tab);
 cudaError_t upload_tables_convert(int n, const void *tab);
 cudaError_t upload_tables_batch(int n, const void *tab);
 cudaError_t upload_tables_solver(int n, const void *tab);
+cudaError_t upload_tables_probe_fx(int n, const void *tab);
 
 /* Scratch for one call, carved from a per-device workspace. */
 struct Workspace {
@@ -76,8 +77,11 @@ cudaError_t launch_pack(int nmod, bool to_soa, void *aos, const mp_array_t &a, l
 
 cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, void *r, long long count,
                                cudaStream_t s);
-cudaError_t launch_chain_probe(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
-                               unsigned *rounds, void *res, cudaStream_t s);
+/* the chain latency probe with the FP64 (elementwise.cu) or fixed-point (probe_fx.cu) evaluation */
+cudaError_t launch_chain_probe_fp64(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
+                                    unsigned *rounds, void *res, cudaStream_t s);
+cudaError_t launch_chain_probe_fx(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
+                                  unsigned *rounds, void *res, cudaStream_t s);
 cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,
                              cudaStream_t s);
 cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void *out, long long count,

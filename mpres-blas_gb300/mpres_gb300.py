@@ -702,12 +702,13 @@ def probe_ceil_log2(x):
     return do.to_numpy(np.float64, x.size)
 
 
-PROBE_MUL_ADD, PROBE_ADD, PROBE_MULD_ADD = 0, 1, 2
+PROBE_MUL_ADD, PROBE_ADD, PROBE_MULD_ADD, PROBE_FIXED_POINT = 0, 1, 2, 16
 
 
 def probe_chain(nmod, kind, x, y, length):
     """One warp's reduction chains (mpres_probe_chain): x, y host arrays of
-    32*length records (y doubles for PROBE_MULD_ADD, unused for PROBE_ADD).
+    32*length records (y doubles for PROBE_MULD_ADD, unused for PROBE_ADD);
+    kind + PROBE_FIXED_POINT evaluates intervals in fixed point.
     Returns (cycles per step, lanes whose product rounded, lanes whose sum
     rounded, the 32 chains' sums)."""
     import torch

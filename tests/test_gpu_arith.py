@@ -152,17 +152,19 @@ def test_ceil_log2_of_doubles_matches_cuda(gpu):
     assert len(bad) == 0, [(float.hex(float(allx[i])), out[i].tolist()) for i in bad[:5]]
 
 
-@pytest.mark.parametrize("n,kind", [(8, 0), (8, 1), (8, 2), (16, 0), (32, 2)])
+@pytest.mark.parametrize("n,kind", [(8, 0), (8, 1), (8, 2), (16, 0), (32, 2), (8, 16), (8, 18), (16, 17)])
 def test_chain_probe_computes_the_chains(gpu, oracle, n, kind):
-    """The latency probe runs the real reduction step: each lane's chain sum
-    equals the oracle's sequential chain, and it reports at least one cycle
-    per step and round counts no larger than the warp."""
+    """The latency probe runs the real reduction step, with the FP64 or (kind +
+    16) the fixed-point interval evaluation: each lane's chain sum equals the
+    oracle's sequential chain, and it reports at least one cycle per step and
+    round counts no larger than the warp."""
+    fixed, kind = kind >= 16, kind % 16
     rng = np.random.default_rng(helpers.SEED + 950 + n + kind)
     length = 40
     x = gpu.set_d(n, helpers.doubles(rng, 32 * length, -16, 16))
     y = (helpers.doubles(rng, 32 * length, -8, 8) if kind == 2
          else gpu.set_d(n, helpers.doubles(rng, 32 * length, -16, 16)) if kind == 0 else None)
-    cycles, prod_rounds, sum_rounds, res = gpu.probe_chain(n, kind, x, y, length)
+    cycles, prod_rounds, sum_rounds, res = gpu.probe_chain(n, kind + 16 * fixed, x, y, length)
     acc = np.zeros(32, x.dtype)
     acc["eval"]["frac"] = 0.0
     for t in range(length):
