@@ -40,6 +40,8 @@
  * interval evaluation (out-of-line steps, epilogue, step-by-step chain) runs in
  * fixed point on the integer pipes (mp_device.cuh) */
 #define MPRES_EVAL_FIXED_POINT 1
+#include <cstdlib>
+
 #include "kernels.h"
 #include "mp_device.cuh"
 
@@ -424,6 +426,229 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, S
     store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
 }
 
+/* ------------------- the k chain with shared-memory k tiles ------------------
+ *
+ * The same lazy-residue chain as gemm_nn_lazy, with its operands staged: for
+ * every KT consecutive k steps the block copies, with cp.async into a second
+ * buffer while it works on the first,
+ *   W(A) of its 32 rows (KT x N/4 x 32 int4), W(B) of its 4 columns
+ *   (KT x 4 x N/4 int4), and the sign, exponent and interval of those A and B
+ *   elements;
+ * each thread then reads its residues one quad at a time (its row's quad and
+ * the column's quad, a broadcast) right where they are accumulated.  W(A) is
+ * read from L2 once per block instead of once per warp, and only one quad of
+ * residues is live at a time: at most 128 registers, so four blocks fit on an
+ * SM.  Blocks walk C in groups of kGroupRows row blocks, so the blocks resident
+ * at once share their rows of W(A) and columns of W(B) in L2. */
+constexpr int kKT = 4;          /* k steps per staged tile */
+constexpr int kGroupRows = 8;   /* row blocks per group of the block order */
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, bool ok) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, bool ok) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(ok ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void lds128(uint32_t addr, uint32_t &a, uint32_t &b, uint32_t &c, uint32_t &d) {
+    asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(a), "=r"(b), "=r"(c), "=r"(d) : "r"(addr));
+}
+
+/* one buffer of a k tile */
+template <int N, int BX, int BY> struct GemmTile {
+    int4 wa[kKT][N / 4][BX];
+    int4 wb[kKT][BY][N / 4];
+    longlong2 aev[kKT][2][BX]; /* lower, upper bound of A(row, k) */
+    longlong2 bev[kKT][2][BY];
+    int as[kKT][BX], ae[kKT][BX];
+    int bs[kKT][BY], be[kKT][BY];
+};
+
+template <int N, int BX, int BY>
+__device__ __forceinline__ void stage_tile(GemmTile<N, BX, BY> &tl, int k0, int m, int n, int k, int r0, int c0,
+                                           SoA A, int lda, int lenA, SoA B, int ldb, int lenB, const int4 *WA,
+                                           const int4 *WB) {
+    constexpr int Q = N / 4, T = BX * BY;
+    const int t = threadIdx.y * BX + threadIdx.x;
+    const int4 *wa0 = WA, *wb0 = WB;
+    for (int e = t; e < kKT * Q * BX; e += T) {
+        const int r = e % BX, q = (e / BX) % Q, kk = e / (BX * Q);
+        const bool ok = (k0 + kk < k) && (r0 + r < m);
+        const int4 *src = ok ? WA + ((size_t)(k0 + kk) * Q + q) * m + r0 + r : wa0;
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.wa[kk][q][r]), src, ok);
+    }
+    for (int e = t; e < kKT * BY * Q; e += T) {
+        const int q = e % Q, kk = (e / Q) % kKT, cy = e / (Q * kKT);
+        const bool ok = (k0 + kk < k) && (c0 + cy < n);
+        const int4 *src = ok ? WB + ((size_t)(c0 + cy) * k + k0 + kk) * Q + q : wb0;
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.wb[kk][cy][q]), src, ok);
+    }
+    const longlong2 *aev = reinterpret_cast<const longlong2 *>(A.eval);
+    const longlong2 *bev = reinterpret_cast<const longlong2 *>(B.eval);
+    for (int e = t; e < kKT * BX; e += T) {
+        const int r = e % BX, kk = e / BX;
+        const bool ok = (k0 + kk < k) && (r0 + r < m);
+        const long long i = ok ? (long long)lda * (k0 + kk) + r0 + r : 0;
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.as[kk][r]), A.sign + i, ok);
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.ae[kk][r]), A.exp + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.aev[kk][0][r]), aev + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.aev[kk][1][r]), aev + lenA + i, ok);
+    }
+    for (int e = t; e < kKT * BY; e += T) {
+        const int kk = e % kKT, cy = e / kKT;
+        const bool ok = (k0 + kk < k) && (c0 + cy < n);
+        const long long i = ok ? (long long)ldb * (c0 + cy) + k0 + kk : 0;
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.bs[kk][cy]), B.sign + i, ok);
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.be[kk][cy]), B.exp + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.bev[kk][0][cy]), bev + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.bev[kk][1][cy]), bev + lenB + i, ok);
+    }
+}
+
+template <int N, int BX, int BY, int MINB>
+__global__ void __launch_bounds__(BX *BY, MINB) gemm_nn_tiled(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
+                                                          int ldb, SoA beta, int *cd, int *cs, int *ce, er_t *cv,
+                                                          const int *clen, int ldc, const int4 *WA, const int4 *WB) {
+    constexpr int Q = N / 4;
+    extern __shared__ __align__(16) unsigned char gemm_smem[];
+    GemmTile<N, BX, BY> *tiles = reinterpret_cast<GemmTile<N, BX, BY> *>(gemm_smem);
+    const Tables<N> &t = T<N>();
+    /* block order: groups of kGroupRows row blocks, column blocks inside a group */
+    const int gx = (m + BX - 1) / BX, gy = (n + BY - 1) / BY;
+    const int per_group = kGroupRows * gy;
+    const int grp = blockIdx.x / per_group, in = blockIdx.x % per_group;
+    const int rows_in_group = min(kGroupRows, gx - grp * kGroupRows);
+    const int bx = grp * kGroupRows + in % rows_in_group, by = in / rows_in_group;
+    const int r0 = bx * BX, c0 = by * BY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int row = r0 + tx, col = c0 + ty;
+    const bool live = row < m && col < n;
+    const int lenA = __ldg(A.len), lenB = __ldg(B.len);
+    uint64_t acc[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) acc[i] = 0;
+    Scal sum;
+    sum.sign = 0;
+    sum.exp = 0;
+    sum.ev[0].frac = 0.0; sum.ev[0].exp = 0;
+    sum.ev[1].frac = 0.0; sum.ev[1].exp = 0;
+    int since_fold = 0;
+    const int ntiles = (k + kKT - 1) / kKT;
+    stage_tile<N, BX, BY>(tiles[0], 0, m, n, k, r0, c0, A, lda, lenA, B, ldb, lenB, WA, WB);
+    cp_async_commit();
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int buf = tile & 1;
+        if (tile + 1 < ntiles)
+            stage_tile<N, BX, BY>(tiles[buf ^ 1], (tile + 1) * kKT, m, n, k, r0, c0, A, lda, lenA, B, ldb, lenB, WA,
+                                  WB);
+        cp_async_commit();
+        cp_async_wait_one();
+        __syncthreads();
+        const GemmTile<N, BX, BY> &tl = tiles[buf];
+        const int k0 = tile * kKT;
+        const int kend = min(kKT, k - k0);
+        if (live) {
+            const uint32_t wa_s = (uint32_t)__cvta_generic_to_shared(&tl.wa[0][0][tx]);
+            const uint32_t wb_s = (uint32_t)__cvta_generic_to_shared(&tl.wb[0][ty][0]);
+            /* the steps that stay lazy run in the inner loop, which leaves at the
+             * first that does not; that step runs out of line (as in gemm_nn_lazy) */
+            int kk = 0;
+            for (;;) {
+                for (; kk < kend; kk++) {
+                    const longlong2 a0 = tl.aev[kk][0][tx], a1 = tl.aev[kk][1][tx];
+                    const longlong2 b0 = tl.bev[kk][0][ty], b1 = tl.bev[kk][1][ty];
+                    const int sa = tl.as[kk][tx], ea = tl.ae[kk][tx], sb = tl.bs[kk][ty], eb = tl.be[kk][ty];
+                    const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
+                    const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
+                    /* mp_mul without residues */
+                    Scal p;
+                    p.sign = sa ^ sb;
+                    p.exp = ea + eb;
+                    p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                    p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                    Scal r;
+                    int nzx, nzy;
+                    const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
+                    const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
+                                      small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
+                    if (!lazy) break;
+                    if (!nzx) {
+#pragma unroll
+                        for (int j = 0; j < N; j++) acc[j] = 0;
+                    }
+                    if (nzy) {
+                        const uint32_t ua = wa_s + (uint32_t)(kk * Q * BX * 16);
+                        const uint32_t ub = wb_s + (uint32_t)(kk * BY * Q * 16);
+#pragma unroll
+                        for (int q = 0; q < Q; q++) {
+                            uint32_t u0, u1, u2, u3, v0, v1, v2, v3;
+                            lds128(ua + (uint32_t)(q * BX * 16), u0, u1, u2, u3);
+                            lds128(ub + (uint32_t)(q * 16), v0, v1, v2, v3);
+                            acc[4 * q] += (uint64_t)u0 * v0;
+                            acc[4 * q + 1] += (uint64_t)u1 * v1;
+                            acc[4 * q + 2] += (uint64_t)u2 * v2;
+                            acc[4 * q + 3] += (uint64_t)u3 * v3;
+                        }
+                    }
+                    sum = r;
+                    if (++since_fold == kFoldEvery) {
+                        since_fold = 0;
+#pragma unroll
+                        for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
+                    }
+                }
+                if (kk >= kend) break;
+                {
+                    uint64_t w[N]; /* copies: see round_if_needed */
+                    Scal sc = sum;
+#pragma unroll
+                    for (int j = 0; j < N; j++) w[j] = acc[j];
+                    full_step<N>(w, &sc, A, (long long)lda * (k0 + kk) + row, lenA, B,
+                                 (long long)col * ldb + k0 + kk, lenB);
+#pragma unroll
+                    for (int j = 0; j < N; j++) acc[j] = w[j];
+                    sum = sc;
+                }
+                if (++since_fold == kFoldEvery) {
+                    since_fold = 0;
+#pragma unroll
+                    for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
+                }
+                kk++;
+            }
+        }
+        __syncthreads(); /* the buffer is restaged by the next iteration */
+    }
+    cp_async_wait_all();
+    if (!live) return;
+    mp_t<N> s;
+    {
+        uint64_t w[N];
+        int d[N];
+#pragma unroll
+        for (int j = 0; j < N; j++) w[j] = acc[j];
+        residues_from_acc<N>(d, w, sum.sign, sum.exp);
+#pragma unroll
+        for (int j = 0; j < N; j++) s.d[j] = d[j];
+    }
+    s.sign = sum.sign;
+    s.exp = sum.exp;
+    s.ev[0] = sum.ev[0];
+    s.ev[1] = sum.ev[1];
+    const int lenC = __ldg(clen);
+    const long long ic = (long long)col * ldc + row;
+    mp_t<N> al, be, buf, c0v, cb, res;
+    load_soa<N>(al, alpha.digits, alpha.sign, alpha.exp, alpha.eval, __ldg(alpha.len), 0);
+    load_soa<N>(be, beta.digits, beta.sign, beta.exp, beta.eval, __ldg(beta.len), 0);
+    mp_mul<N>(buf, s, al);
+    load_soa<N>(c0v, cd, cs, ce, cv, lenC, ic);
+    mp_mul<N>(cb, c0v, be);
+    split_add<N>(res, cb, buf);
+    store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
+}
+
 template <int N>
 cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda, const mp_array_t &B,
                 int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s) {
@@ -436,8 +661,33 @@ cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &
         const long long na = (long long)m * k, nb = (long long)k * n;
         gemm_prescale<N, true><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A.digits, A.sign, A.exp, lda, m, k, wa);
         gemm_prescale<N, false><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, wb);
-        gemm_nn_lazy<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta),
-                                                       C.digits, C.sign, C.exp, cv, C.len, ldc, wa, wb);
+        const char *v1 = std::getenv("MPRES_GEMM_V1");
+        if (v1 && v1[0] == '1') {
+            gemm_nn_lazy<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta),
+                                                           C.digits, C.sign, C.exp, cv, C.len, ldc, wa, wb);
+        } else {
+            constexpr size_t smem = 2 * sizeof(GemmTile<N, BX, BY>);
+            const char *mb = std::getenv("MPRES_GEMM_MINB");
+            const bool three = mb && mb[0] == '3';
+            static PerDevice<cudaError_t> attrs(cuda_ok);
+            cudaError_t e = attrs.get(current_device(), cudaErrorInvalidDevice, [] {
+                cudaError_t r = cudaFuncSetAttribute(gemm_nn_tiled<N, BX, BY, 4>,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (r != cudaSuccess) return r;
+                return cudaFuncSetAttribute(gemm_nn_tiled<N, BX, BY, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem);
+            });
+            if (e != cudaSuccess) return e;
+            const unsigned blocks = grid.x * grid.y;
+            if (three)
+                gemm_nn_tiled<N, BX, BY, 3><<<blocks, block, smem, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb,
+                                                                        soa(beta), C.digits, C.sign, C.exp, cv, C.len,
+                                                                        ldc, wa, wb);
+            else
+                gemm_nn_tiled<N, BX, BY, 4><<<blocks, block, smem, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb,
+                                                                        soa(beta), C.digits, C.sign, C.exp, cv, C.len,
+                                                                        ldc, wa, wb);
+        }
     } else {
         gemm_nn<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta), C.digits,
                                                   C.sign, C.exp, cv, C.len, ldc);
