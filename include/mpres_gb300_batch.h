@@ -1,7 +1,7 @@
 /*
- * mpres_gb300 batches: many mp_gemv / mp_dot / mp_spmv_csr operations of uneven
- * sizes run as ONE persistent kernel launch, replayed from a captured CUDA
- * graph.  No counterpart in the reference, which launches every operation on
+ * mpres_gb300 batches: many mp_gemv / mp_dot / mp_spmv (CSR, CSR-vector, ELL)
+ * operations of uneven sizes run as ONE persistent kernel launch, replayed
+ * from a captured CUDA graph.  No counterpart in the reference, which launches every operation on
  * its own (cuda::mp_gemv, src/blas/gemv.cuh:151-269: ten kernels per call;
  * cuda::mp_dot, src/blas/dot.cuh:85-108; cuda::mp_spmv_csr,
  * src/sparse/spmv/spmv_csr.cuh:49-63).
@@ -23,8 +23,9 @@
  * list sorted by estimated length, longest first: tiles of R outputs of a
  * GEMV (R = threads / blockDim3), groups of first-pass blocks of a DOT (the CTA
  * that finishes a DOT's last group also runs its second pass), and chunks of
- * length-sorted rows of an SpMV.  GEMV's alpha*x runs as one element-wise
- * launch before it (two kernel nodes and two memset nodes per graph).
+ * length-sorted rows of an SpMV (threads / threadsPerRow rows for CSR-vector).
+ * GEMV's alpha*x runs as one element-wise launch before it (two kernel nodes
+ * and two memset nodes per graph).
  */
 #ifndef MPRES_GB300_BATCH_H
 #define MPRES_GB300_BATCH_H
@@ -54,6 +55,15 @@ int mpres_batch_add_dot(mpres_batch_t *batch, int n, const mp_array_t *x, int in
                         const mp_array_t *r, int gridDim3, int blockDim3);
 /* Same as mpres_spmv_csr: y[0..m) = A*x with AoS mp_float_t vectors. */
 int mpres_batch_add_spmv_csr(mpres_batch_t *batch, int m, const csr_t *csr, const void *x, void *y);
+/* Same as mpres_spmv_csrv (cuda::mp_spmv_csrv<threads, threadsPerRow>,
+ * src/sparse/spmv/spmv_csrv.cuh:49-86): threadsPerRow lane-strided chains per
+ * row and the fixed tree; threadsPerRow a power of two <= 32. */
+int mpres_batch_add_spmv_csrv(mpres_batch_t *batch, int m, const csr_t *csr, const void *x, void *y,
+                              int threadsPerRow);
+/* Same as mpres_spmv_ell (cuda::mp_spmv_ell<threads>, src/sparse/spmv/spmv_ell.cuh:50-67):
+ * maxnzr column-major slots per row, stored zeros skipped.  The commit reads
+ * the slots once to order the rows by length. */
+int mpres_batch_add_spmv_ell(mpres_batch_t *batch, int m, int maxnzr, const ell_t *ell, const void *x, void *y);
 
 int mpres_batch_commit(mpres_batch_t *batch, unsigned flags, void *stream);
 int mpres_batch_run(mpres_batch_t *batch, void *stream);

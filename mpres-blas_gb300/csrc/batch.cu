@@ -1,5 +1,5 @@
 /*
- * Batches of mp_gemv / mp_dot / mp_spmv_csr in one persistent launch
+ * Batches of mp_gemv / mp_dot / mp_spmv_csr / csrv / ell in one persistent launch
  * (include/mpres_gb300_batch.h).  No reference counterpart: the reference
  * launches each operation separately (src/blas/gemv.cuh:151-269,
  * src/blas/dot.cuh:85-108, src/sparse/spmv/spmv_csr.cuh:49-63).
@@ -12,7 +12,9 @@
  *   DOT   gridDim3 first-pass blocks of blockDim3 chains (thread p of the
  *         whole grid takes products p, p + K, ...), a tree per block, then one
  *         block of blockDim3 chains and a tree over the block sums;
- *   SpMV  per row, one chain over its nonzeros.
+ *   SpMV  per row, one chain over its nonzeros (CSR; ELL over its slots,
+ *         stored zeros skipped), or tpr lane-strided chains and the fixed
+ *         16/8/4/2/1 tree (CSR-vector).
  * What the batch chooses -- threads per CTA, CTAs per SM, which CTA runs which
  * tile and when -- never changes a result.
  *
@@ -200,21 +202,97 @@ __device__ __forceinline__ void dot_group(const DotOp &d, int dop, int b0, int n
     if (t == 0) store_soa<N>(sdata[0], d.rd, d.rs, d.re, d.rv, __ldg(d.rlen), 0);
 }
 
+/* shuffle a whole number down by delta lanes */
+template <int N> __device__ __forceinline__ mp_t<N> shfl_down(const mp_t<N> &v, int delta) {
+    mp_t<N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = __shfl_down_sync(0xffffffffu, v.d[i], delta);
+    r.sign = __shfl_down_sync(0xffffffffu, v.sign, delta);
+    r.exp = __shfl_down_sync(0xffffffffu, v.exp, delta);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        r.ev[k].frac = __shfl_down_sync(0xffffffffu, v.ev[k].frac, delta);
+        r.ev[k].exp = __shfl_down_sync(0xffffffffu, v.ev[k].exp, delta);
+    }
+    return r;
+}
+
+/* `rows` rows of the length-sorted order from `first`, in the operation's form
+ * (spmv.cu: spmv_csr_kernel, spmv_csrv_kernel, spmv_ell_kernel); every thread of
+ * the CTA calls it (the CSR-vector tree shuffles across whole warps) */
 template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int first, int rows) {
     const int t = threadIdx.x;
+    if (s.form == kCsrv) {
+        const int tpr = s.tpr, group = t / tpr, sub = t % tpr;
+        const bool active = group < rows;
+        const int row = active ? __ldg(s.perm + first + group) : 0;
+        mp_t<N> sum;
+        set_zero<N>(sum);
+        if (active) {
+            const int start = __ldg(s.irp + row), end = __ldg(s.irp + row + 1);
+            for (int i = start + sub; i < end; i += tpr) {
+                mp_t<N> xv, p, q;
+                load_aos<N>(xv, s.x, __ldg(s.ja + i));
+                mp_mul_d<N>(p, xv, __ldg(s.as + i));
+                mp_add<N>(q, sum, p);
+                sum = q;
+            }
+        }
+        /* the fixed tree of src/sparse/spmv/spmv_csrv.cuh:70-84 */
+        for (int sft = 16; sft >= 1; sft >>= 1) {
+            if (tpr >= 2 * sft) {
+                mp_t<N> other = shfl_down<N>(sum, sft);
+                if (active && sub < sft) {
+                    mp_t<N> q;
+                    mp_add<N>(q, sum, other);
+                    sum = q;
+                }
+            }
+        }
+        if (active && sub == 0) store_aos<N>(sum, s.y, row);
+        return;
+    }
     if (t >= rows) return;
     const int row = __ldg(s.perm + first + t);
     mp_t<N> sum;
     set_zero<N>(sum);
-    const int start = __ldg(s.irp + row), end = __ldg(s.irp + row + 1);
-    for (int i = start; i < end; i++) {
-        mp_t<N> xv, p, q;
-        load_aos<N>(xv, s.x, __ldg(s.ja + i));
-        mp_mul_d<N>(p, xv, __ldg(s.as + i));
-        mp_add<N>(q, sum, p);
-        sum = q;
+    if (s.form == kEll) {
+        for (int col = 0; col < s.maxnzr; col++) {
+            const size_t slot = (size_t)col * s.m + row;
+            const double val = __ldg(s.as + slot);
+            if (dnz(val)) {
+                mp_t<N> xv, p, q;
+                load_aos<N>(xv, s.x, __ldg(s.ja + slot));
+                mp_mul_d<N>(p, xv, val);
+                mp_add<N>(q, sum, p);
+                sum = q;
+            }
+        }
+    } else {
+        const int start = __ldg(s.irp + row), end = __ldg(s.irp + row + 1);
+        for (int i = start; i < end; i++) {
+            mp_t<N> xv, p, q;
+            load_aos<N>(xv, s.x, __ldg(s.ja + i));
+            mp_mul_d<N>(p, xv, __ldg(s.as + i));
+            mp_add<N>(q, sum, p);
+            sum = q;
+        }
     }
     store_aos<N>(sum, s.y, row);
+}
+
+/* ELL row lengths for the schedule: the first empty slot, by bisection as if
+ * the stored entries of a row formed a prefix (spmv.cu's EllLen) */
+__global__ void ell_row_lengths(const double *as, int m, int maxnzr, int *len) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        int lo = 0, hi = maxnzr;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (dnz(__ldg(as + (size_t)mid * m + r))) lo = mid + 1;
+            else hi = mid;
+        }
+        len[r] = lo;
+    }
 }
 
 template <int N, int MAXT> __global__ void __launch_bounds__(MAXT) batch_kernel(BatchArgs a) {
@@ -357,11 +435,23 @@ bool batch_add_dot(BatchHost &b, int n, const mp_array_t &x, int incx, const mp_
 }
 
 void batch_add_spmv(BatchHost &b, int m, const csr_t &csr, const void *x, void *y, const int *perm,
-                    std::vector<int> lens) {
+                    std::vector<int> lens, int form, int tpr) {
     SpmvOp sp{};
     sp.irp = csr.irp; sp.ja = csr.ja; sp.as = csr.as; sp.x = x; sp.y = y; sp.m = m; sp.perm = perm;
+    sp.form = form;
+    sp.tpr = tpr;
     b.spmv.push_back(sp);
     b.spmv_len.push_back(std::move(lens));
+}
+
+void batch_add_spmv_ell(BatchHost &b, int m, int maxnzr, const ell_t &ell, const void *x, void *y) {
+    SpmvOp sp{};
+    sp.ja = ell.ja; sp.as = ell.as; sp.x = x; sp.y = y; sp.m = m;
+    sp.form = kEll;
+    sp.tpr = 1;
+    sp.maxnzr = maxnzr;
+    b.spmv.push_back(sp);
+    b.spmv_len.push_back({});
 }
 
 void spmv_row_order(const int *irp, int m, std::vector<int> &order, std::vector<int> &lens) {
@@ -406,8 +496,14 @@ bool batch_plan(BatchHost &b, int threads) {
     for (size_t i = 0; i < b.spmv.size(); i++) {
         const SpmvOp &sp = b.spmv[i];
         const std::vector<int> &len = b.spmv_len[i];
-        for (int r = 0; r < sp.m; r += threads)
-            items.push_back({(long long)len[r] + 1, {kSpmvChunk, (int)i, r, std::min(threads, sp.m - r)}});
+        if (sp.form == kCsrv && sp.tpr > threads) return false;
+        /* rows per task: one thread per row, or tpr threads per row */
+        const int rows = sp.form == kCsrv ? threads / sp.tpr : threads;
+        for (int r = 0; r < sp.m; r += rows) {
+            long long cost = (long long)len[r] + 1;
+            if (sp.form == kCsrv) cost = (len[r] + sp.tpr - 1) / sp.tpr + (32 - __builtin_clz((unsigned)sp.tpr));
+            items.push_back({cost, {kSpmvChunk, (int)i, r, std::min(rows, sp.m - r)}});
+        }
     }
     std::stable_sort(items.begin(), items.end(), [](const Item &x, const Item &y) { return x.cost > y.cost; });
     b.tasks.resize(items.size());
@@ -608,6 +704,25 @@ int mpres_batch_add_spmv_csr(mpres_batch_t *b, int m, const csr_t *csr, const vo
     return status_ok();
 }
 
+int mpres_batch_add_spmv_csrv(mpres_batch_t *b, int m, const csr_t *csr, const void *x, void *y, int threadsPerRow) {
+    if (int st = check_open(b, "mpres_batch_add_spmv_csrv")) return st;
+    if (threadsPerRow < 1 || threadsPerRow > 32 || (threadsPerRow & (threadsPerRow - 1)))
+        return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_batch_add_spmv_csrv: threadsPerRow %d not a power of two <= 32",
+                           threadsPerRow);
+    if (m <= 0) return status_ok();
+    if (!csr || !x || !y) return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_batch_add_spmv_csrv: null argument");
+    batch_add_spmv(b->host, m, *csr, x, y, nullptr, {}, kCsrv, threadsPerRow);
+    return status_ok();
+}
+
+int mpres_batch_add_spmv_ell(mpres_batch_t *b, int m, int maxnzr, const ell_t *ell, const void *x, void *y) {
+    if (int st = check_open(b, "mpres_batch_add_spmv_ell")) return st;
+    if (m <= 0) return status_ok();
+    if (maxnzr < 0 || !ell || !x || !y) return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_batch_add_spmv_ell: bad argument");
+    batch_add_spmv_ell(b->host, m, maxnzr, *ell, x, y);
+    return status_ok();
+}
+
 int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
     if (int st = check_open(b, "mpres_batch_commit")) return st;
     int dev = 0;
@@ -624,8 +739,24 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
     for (size_t i = 0; i < h.spmv.size(); i++) {
         SpmvOp &sp = h.spmv[i];
         std::vector<int> irp((size_t)sp.m + 1), order;
-        if ((e = cudaMemcpy(irp.data(), sp.irp, sizeof(int) * irp.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        if (sp.form == kEll) {
+            /* ELL: row lengths found on the device, as row pointers for the order */
+            int *dlen = nullptr;
+            std::vector<int> len((size_t)sp.m);
+            if ((e = cudaMalloc(&dlen, sizeof(int) * (size_t)sp.m)) != cudaSuccess)
+                return status_cuda(e, "mpres_batch_commit (ELL row lengths)");
+            ell_row_lengths<<<std::min(4096, (sp.m + 255) / 256), 256, 0, s>>>(sp.as, sp.m, sp.maxnzr, dlen);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e == cudaSuccess) e = cudaMemcpy(len.data(), dlen, sizeof(int) * len.size(), cudaMemcpyDeviceToHost);
+            cudaFree(dlen);
+            if (e != cudaSuccess) return status_cuda(e, "mpres_batch_commit (ELL row lengths)");
+            irp[0] = 0;
+            for (int r = 0; r < sp.m; r++) irp[(size_t)r + 1] = irp[r] + len[r];
+        } else if ((e = cudaMemcpy(irp.data(), sp.irp, sizeof(int) * irp.size(), cudaMemcpyDeviceToHost)) !=
+                   cudaSuccess) {
             return status_cuda(e, "mpres_batch_commit (row pointers)");
+        }
         spmv_row_order(irp.data(), sp.m, order, h.spmv_len[i]);
         perm_off.push_back(perm_all.size());
         perm_all.insert(perm_all.end(), order.begin(), order.end());
@@ -641,10 +772,11 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
         return status_cuda(e, "mpres_batch_commit (alpha*x)");
     if (h.part_elems && (e = cudaMalloc(&b->parts, rec * h.part_elems)) != cudaSuccess)
         return status_cuda(e, "mpres_batch_commit (block sums)");
-    /* launch shape: the largest blockDim3 is the least threads per CTA */
+    /* launch shape: the largest blockDim3 (or threadsPerRow) is the least threads per CTA */
     int min_threads = 32;
     for (const GemvOp &g : h.gemv) min_threads = std::max(min_threads, g.b3);
     for (const DotOp &d : h.dot) min_threads = std::max(min_threads, d.b3);
+    for (const SpmvOp &sp : h.spmv) min_threads = std::max(min_threads, sp.tpr);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     std::vector<std::pair<int, int>> cand; /* threads, CTAs per SM */

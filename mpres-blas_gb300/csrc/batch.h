@@ -2,8 +2,9 @@
  * Internal interface of the persistent batch kernel (batch.cu), shared by the
  * batch entry points (mpres_batch_*) and the serving loop (server.cpp).
  *
- * A batch is a list of operations (GEMV, DOT, SpMV CSR) with device pointers to
- * their operands, a task list over them, and scratch: GEMV's alpha*x
+ * A batch is a list of operations (GEMV, DOT, SpMV in its CSR, CSR-vector and
+ * ELL forms) with device pointers to their operands, a task list over them,
+ * and scratch: GEMV's alpha*x
  * (`buf1`, one record per inner index) and DOT's block sums (`parts`, gridDim3
  * records per DOT).  The host builds everything in BatchHost; the device copy
  * of the tables lives wherever the caller put it (BatchDev).
@@ -54,13 +55,18 @@ struct DotOp {
     long long part_off;
 };
 
+/* SpMV forms: CSR (one chain per row), CSR-vector (tpr lane-strided chains
+ * per row and the fixed tree), ELL (one chain per row over column-major slots,
+ * stored zeros skipped; irp unused) */
+enum SpmvForm { kCsr = 0, kCsrv = 1, kEll = 2 };
+
 struct SpmvOp {
     const int *irp, *ja;
     const double *as;
     const void *x;
     void *y;
     const int *perm; /* rows by length, longest first */
-    int m, pad;
+    int m, form, tpr, maxnzr;
 };
 
 enum TaskKind { kGemvTile = 0, kDotGroup = 1, kSpmvChunk = 2 };
@@ -100,7 +106,8 @@ bool batch_add_gemv(BatchHost &b, int trans, int m, int n, const mp_array_t &alp
 bool batch_add_dot(BatchHost &b, int n, const mp_array_t &x, int incx, const mp_array_t &y, int incy,
                    const mp_array_t &r, int g3, int b3);
 void batch_add_spmv(BatchHost &b, int m, const csr_t &csr, const void *x, void *y, const int *perm,
-                    std::vector<int> lens);
+                    std::vector<int> lens, int form = kCsr, int tpr = 1);
+void batch_add_spmv_ell(BatchHost &b, int m, int maxnzr, const ell_t &ell, const void *x, void *y);
 
 /* rows of a CSR matrix by length, longest first, equal lengths in row order,
  * from host row pointers; lens[i] = length of row order[i] */

@@ -87,6 +87,8 @@ _SIGS = {
     "mpres_batch_add_gemv": (I, [P, I, I, I, P, P, I, P, I, P, P, I, I]),
     "mpres_batch_add_dot": (I, [P, I, P, I, P, I, P, I, I]),
     "mpres_batch_add_spmv_csr": (I, [P, I, P, P, P]),
+    "mpres_batch_add_spmv_csrv": (I, [P, I, P, P, P, I]),
+    "mpres_batch_add_spmv_ell": (I, [P, I, I, P, P, P]),
     "mpres_batch_commit": (I, [P, ctypes.c_uint, P]),
     "mpres_batch_run": (I, [P, P]),
     "mpres_batch_info": (I, [P, P]),
@@ -562,6 +564,16 @@ class Batch:
         self._keep += [csr, x, y]
         check(lib().mpres_batch_add_spmv_csr(self.h, m, ctypes.byref(csr.c), x.ptr, y.ptr),
               "mpres_batch_add_spmv_csr")
+
+    def add_spmv_csrv(self, m, csr, x, y, tpr):
+        self._keep += [csr, x, y]
+        check(lib().mpres_batch_add_spmv_csrv(self.h, m, ctypes.byref(csr.c), x.ptr, y.ptr, tpr),
+              "mpres_batch_add_spmv_csrv")
+
+    def add_spmv_ell(self, m, ell, x, y):
+        self._keep += [ell, x, y]
+        check(lib().mpres_batch_add_spmv_ell(self.h, m, ell.maxnzr, ctypes.byref(ell.e), x.ptr, y.ptr),
+              "mpres_batch_add_spmv_ell")
 
     def commit(self, flags=BATCH_GRAPH, stream=None):
         check(lib().mpres_batch_commit(self.h, flags, _stream_handle(stream)), "mpres_batch_commit")

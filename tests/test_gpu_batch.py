@@ -1,8 +1,8 @@
 """Batches (one persistent launch for many operations) against the plain entry
-points: every GEMV, DOT and SpMV output of a batch must equal, record for
-record, what mpres_gemv / mpres_dot / mpres_spmv_csr give for the same
-arguments -- with and without graph replay and autotuning, for uneven sizes,
-strides, transposition, odd blockDim3 and skipped operations."""
+points: every GEMV, DOT and SpMV (CSR, CSR-vector, ELL) output of a batch
+must equal, record for record, what mpres_gemv / mpres_dot / mpres_spmv_* give
+for the same arguments -- with and without graph replay and autotuning, for
+uneven sizes, strides, transposition, odd blockDim3 and skipped operations."""
 import numpy as np
 import pytest
 
@@ -49,6 +49,15 @@ def _build(gpu, n, rng, small):
     m = 3000 // scale
     irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
     ops.append(dict(kind="spmv", m=m, csr=gpu.DeviceCsr(m, irp, ja, vals), x=_vec(gpu, n, rng, m, -16, 16)))
+    for tpr in (2, 16):
+        m = (2000 + 37 * tpr) // scale
+        irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m, kmax=300))
+        ops.append(dict(kind="csrv", tpr=tpr, m=m, csr=gpu.DeviceCsr(m, irp, ja, vals),
+                        x=_vec(gpu, n, rng, m, -16, 16)))
+    m = 1500 // scale
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m, kmax=150))
+    maxnzr, eja, eas = helpers.csr_to_ell(m, irp, ja, vals)
+    ops.append(dict(kind="ell", m=m, ell=gpu.DeviceEll(m, maxnzr, eja, eas), x=_vec(gpu, n, rng, m, -16, 16)))
     return ops
 
 
@@ -70,7 +79,12 @@ def _plain(gpu, n, ops):
         else:
             x = gpu.DeviceBytes.from_numpy(o["x"])
             y = gpu.DeviceBytes(o["m"] * (4 * n + 40))
-            gpu.spmv_csr(n, o["m"], o["csr"], x, y)
+            if o["kind"] == "spmv":
+                gpu.spmv_csr(n, o["m"], o["csr"], x, y)
+            elif o["kind"] == "csrv":
+                gpu.spmv_csrv(n, o["m"], o["csr"], x, y, o["tpr"])
+            else:
+                gpu.spmv_ell(n, o["m"], o["ell"], x, y)
             out.append(y.to_numpy(o["x"].dtype, o["m"]))
     return out
 
@@ -94,7 +108,12 @@ def _batched(gpu, n, ops, flags, runs=1):
         else:
             x = gpu.DeviceBytes.from_numpy(o["x"])
             y = gpu.DeviceBytes(o["m"] * (4 * n + 40))
-            b.add_spmv_csr(o["m"], o["csr"], x, y)
+            if o["kind"] == "spmv":
+                b.add_spmv_csr(o["m"], o["csr"], x, y)
+            elif o["kind"] == "csrv":
+                b.add_spmv_csrv(o["m"], o["csr"], x, y, o["tpr"])
+            else:
+                b.add_spmv_ell(o["m"], o["ell"], x, y)
             outs.append((y, o["m"], o["x"].dtype))
     b.commit(flags)
     for _ in range(runs):
@@ -112,7 +131,7 @@ def test_batch_matches_plain_calls(gpu, n, flags):
     want = _plain(gpu, n, ops)
     got, info = _batched(gpu, n, ops, flags)
     live = [o for o in ops if (o["kind"] == "gemv" and o["m"] > 0 and o["n"] > 0 and o["incx"] and o["incy"])
-            or (o["kind"] == "dot" and o["n"] > 0) or o["kind"] == "spmv"]
+            or (o["kind"] == "dot" and o["n"] > 0) or o["kind"] in ("spmv", "csrv", "ell")]
     assert info["ops"] == len(live)  # the others are quick returns
     assert info["graph"] == (flags & 1)
     assert info["autotuned"] == (1 if flags & 2 else 0)
