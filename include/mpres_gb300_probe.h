@@ -57,6 +57,15 @@ int mpres_probe_check(int which, int nmod, const void *a, const void *b, void *o
 int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                       unsigned *rounds, void *result, void *stream);
 
+/* Where the time of a rounding goes, one warp alone: digits = int[32*count*nmod]
+ * (lane l takes numbers l*count .. l*count+count-1), D = unsigned[32*count]
+ * bits to round away; cycles = long long[count*5] receives lane 0's SM cycles
+ * per number of {rns_scale2pow, rns_eval_compute_fast, one upward fraction
+ * sum, the modular products of one refinement step, rank_full}; out = int[32]
+ * (a checksum).  Device memory. */
+int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
+                         void *stream);
+
 /* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
  * element per thread: the device functions the BLAS kernels are built from,
  * exposed so that each can be checked against the reference on its own.

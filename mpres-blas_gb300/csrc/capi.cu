@@ -111,6 +111,8 @@ void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, co
     t.host_ceil_log2 = dhost_log2;
     for (int i = 0; i < N; i++) t.recip_rn[i] = 1.0 / (double)h.moduli[i];
     for (int i = 0; i < N; i++) t.pow2_32[i] = (uint32_t)((1ull << 32) % (unsigned long long)h.moduli[i]);
+    for (int i = 0; i < N; i++)
+        t.inv94[i] = (uint64_t)((((unsigned __int128)1) << 94) / (unsigned __int128)(unsigned)h.moduli[i]);
     for (int i = 0; i < N; i++) {
         t.recip_rd_m[i] = h.recip_rd_m[i];
         t.recip_ru_m[i] = h.recip_ru_m[i];
@@ -779,6 +781,15 @@ int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len,
     cudaError_t e = fixed ? launch_chain_probe_fx(nmod, k, x, y, len, cycles, rounds, result, s)
                           : launch_chain_probe_fp64(nmod, k, x, y, len, cycles, rounds, result, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_chain");
+}
+
+int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
+                         void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count <= 0 || !digits || !D || !cycles || !out)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_rounding: bad arguments");
+    cudaError_t e = launch_round_probe(nmod, digits, D, count, cycles, out, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_rounding");
 }
 
 int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {

@@ -78,10 +78,82 @@ __global__ void chain_probe(int kind, const void *x, const void *y, int len, lon
     store_aos<N>(acc, res, lane);
 }
 
+/* Where a rounding's time goes, one warp alone: for `count` numbers per lane
+ * (lane l takes digits of numbers l*count .. l*count+count-1, D[] the bits to
+ * round away) lane 0 records per number the SM cycles of
+ *   [0] rns_scale2pow(d, D), [1] rns_eval_compute_fast(d) (the rounding's two
+ *   halves, mp_device.cuh's scale2pow and eval_fast), [2] one upward pairwise
+ *   fraction sum psum_ru of the rounded residues, [3] the N modular products
+ *   of one refinement step (s_i * RNS_POW2[k][i], k data dependent), and
+ *   [4] rank_full of the input (the first scaling step's rank).
+ * Results are written to `out` so nothing is optimised away. */
+template <int N>
+__global__ void round_parts_probe(const int *digits, const unsigned *D, int count, long long *cycles, int *out) {
+    const Tables<N> &t = T<N>();
+    const int lane = threadIdx.x;
+    int acc = 0;
+    for (int j = 0; j < count; j++) {
+        const long long e = (long long)lane * count + j;
+        int d[N], c[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) d[i] = __ldg(digits + e * N + i);
+        const unsigned bits = __ldg(D + e);
+        __syncwarp();
+        long long t0 = clock64();
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(d[i], t.part_inv[i], i);
+        const int rk = rank_full<N>(d, c);
+        acc += rk;
+        __syncwarp();
+        long long t1 = clock64();
+        scale2pow<N>(d, bits);
+        acc += d[0];
+        __syncwarp();
+        long long t2 = clock64();
+        er_t lo, up;
+        eval_fast<N>(lo, up, d);
+        acc += (int)up.exp;
+        __syncwarp();
+        long long t3 = clock64();
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(d[i], t.part_inv[i], i);
+        const double su = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)c[i]), t.recip_ru[i]); });
+        acc += (int)(dbits(su) >> 40);
+        __syncwarp();
+        long long t4 = clock64();
+        const int k = (int)(dbits(su) >> 52) & 63;
+        const int *row = t.pow2 + (size_t)pow2_row_index<N>(k) * N;
+#pragma unroll
+        for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(c[i], __ldg(row + i), i);
+        acc += c[N - 1];
+        __syncwarp();
+        long long t5 = clock64();
+        if (lane == 0) {
+            cycles[j * 5 + 0] = t2 - t1;
+            cycles[j * 5 + 1] = t3 - t2;
+            cycles[j * 5 + 2] = t4 - t3;
+            cycles[j * 5 + 3] = t5 - t4;
+            cycles[j * 5 + 4] = t1 - t0;
+        }
+    }
+    out[lane] = acc;
+}
+
 } // namespace chainprobe
 } // namespace mpres
 
-/* the host launcher of this translation unit's instantiation */
+/* the host launchers of this translation unit's instantiations */
+#define MPRES_ROUND_PROBE_LAUNCHER(NAME)                                                                      \
+    cudaError_t NAME(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,  \
+                     cudaStream_t s) {                                                                        \
+        switch (nmod) {                                                                                       \
+        case 8: chainprobe::round_parts_probe<8><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;      \
+        case 16: chainprobe::round_parts_probe<16><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;    \
+        case 32: chainprobe::round_parts_probe<32><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;    \
+        default: return cudaErrorInvalidValue;                                                                \
+        }                                                                                                     \
+        return cudaGetLastError();                                                                            \
+    }
 #define MPRES_CHAIN_PROBE_LAUNCHER(NAME)                                                                   \
     cudaError_t NAME(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,         \
                      unsigned *rounds, void *res, cudaStream_t s) {                                        \

@@ -80,6 +80,8 @@ cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, v
 /* the chain latency probe with the FP64 (elementwise.cu) or fixed-point (probe_fx.cu) evaluation */
 cudaError_t launch_chain_probe_fp64(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                                     unsigned *rounds, void *res, cudaStream_t s);
+cudaError_t launch_round_probe(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
+                               cudaStream_t s);
 cudaError_t launch_chain_probe_fx(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                                   unsigned *rounds, void *res, cudaStream_t s);
 cudaError_t launch_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, long long count,

@@ -546,8 +546,33 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
 #endif
 }
 
+/* The rank of a number -- floor(V) for V = sum_i s_i / m_i -- the way the
+ * reference obtains it: the whole parts of the directed-rounding pairwise sums
+ * of the leaves RD/RU(s_i * recip_i) (rank_full compares both, rank_fast takes
+ * the upward one).  Those sums bracket V within 2^-42: each of the N <= 32
+ * leaves is below 1 and errs by less than 2^-53, each of the N - 1 additions
+ * of partial sums below 32 by less than 2^-48.  So whenever frac(V) lies in
+ * [2^-40, 1 - 2^-40] both whole parts equal floor(V), and floor(V) is the
+ * rank exactly.  rank_shortcut decides that from the exact integer sum
+ * S = sum_i s_i * floor(2^94 / m_i) (V - 2^-58 < S / 2^94 <= V): it returns
+ * true with floor(V) in `rank` when the top 42 fraction bits of S keep a
+ * margin of 2^-39 from both integers, and false otherwise -- then the FP64
+ * sums decide, as in the reference.  Integer pipes only, about 40 instructions
+ * instead of one or two 2N-1-operation FP64 sums. */
+template <int N> __device__ __forceinline__ bool rank_shortcut(const int *s, unsigned int &rank) {
+    const Tables<N> &t = T<N>();
+    unsigned __int128 S = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) S += (unsigned __int128)(uint32_t)s[i] * t.inv94[i];
+    const uint64_t top = (uint64_t)(S >> 52) & ((1ull << 42) - 1); /* fraction bits 2^-1 .. 2^-42 */
+    rank = (unsigned int)(S >> 94);
+    return top >= 8 && top <= (1ull << 42) - 9;
+}
+
 /* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */
 template <int N> __device__ __forceinline__ int rank_full(const int *x, const int *s) {
+    unsigned int fast;
+    if (rank_shortcut<N>(s, fast)) return (int)fast;
 #if MPRES_EVAL_FIXED_POINT
     const unsigned int whl = fx_whole(fx_fraction_sum<N, false>(s));
     const unsigned int whu = fx_whole(fx_fraction_sum<N, true>(s));
@@ -561,6 +586,8 @@ template <int N> __device__ __forceinline__ int rank_full(const int *x, const in
 }
 /* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096 */
 template <int N> __device__ __forceinline__ int rank_fast(const int *s) {
+    unsigned int fast;
+    if (rank_shortcut<N>(s, fast)) return (int)fast;
 #if MPRES_EVAL_FIXED_POINT
     return (int)fx_whole(fx_fraction_sum<N, true>(s));
 #else

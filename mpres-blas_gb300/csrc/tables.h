@@ -52,6 +52,7 @@ struct Tables {
     double recip_rn[N];          /* 1.0 / m_i rounded to nearest, as the host computes it */
     const int *host_ceil_log2;   /* device: host_ceil_log2_table() */
     uint32_t pow2_32[N];         /* 2^32 mod m_i: folds a 64-bit residue accumulator */
+    uint64_t inv94[N];           /* floor(2^94 / m_i), 2^63 < inv94 < 2^64: the exact rank shortcut */
 };
 
 /* Host-side copy of every table in the reference's array shapes. */
