@@ -1,13 +1,13 @@
 /*
- * mpres_gb300 batches: many mp_gemv / mp_dot / mp_spmv (CSR, CSR-vector, ELL)
- * operations of uneven sizes run as ONE persistent kernel launch, replayed
- * from a captured CUDA graph.  No counterpart in the reference, which launches every operation on
+ * mpres_gb300 batches: many mp_gemv / mp_gemm / mp_dot / mp_spmv (CSR,
+ * CSR-vector, ELL) operations of uneven sizes run as ONE persistent kernel
+ * launch, replayed from a captured CUDA graph.  No counterpart in the reference, which launches every operation on
  * its own (cuda::mp_gemv, src/blas/gemv.cuh:151-269: ten kernels per call;
  * cuda::mp_dot, src/blas/dot.cuh:85-108; cuda::mp_spmv_csr,
  * src/sparse/spmv/spmv_csr.cuh:49-63).
  *
  * Results.  Every operation of a batch gives, bit for bit, what the plain entry
- * point (mpres_gemv, mpres_dot, mpres_spmv_csr) gives for the same arguments:
+ * point (mpres_gemv, mpres_gemm, mpres_dot, mpres_spmv_*) gives for the same arguments:
  * the summation order of each output is fixed by the operation's own
  * blockDim3 / gridDim3, never by the batch, the launch shape or the autotuner.
  *
@@ -22,9 +22,10 @@
  * Scheduling.  The kernel's CTAs take tasks from one atomic counter over a task
  * list sorted by estimated length, longest first: tiles of R outputs of a
  * GEMV (R = threads / blockDim3), groups of first-pass blocks of a DOT (the CTA
- * that finishes a DOT's last group also runs its second pass), and chunks of
- * length-sorted rows of an SpMV (threads / threadsPerRow rows for CSR-vector).
- * GEMV's alpha*x runs as one element-wise launch before it (two kernel nodes
+ * that finishes a DOT's last group also runs its second pass), chunks of
+ * length-sorted rows of an SpMV (threads / threadsPerRow rows for CSR-vector),
+ * and 32 x (threads / 32) tiles of a GEMM's C.  GEMV's alpha*x and GEMM's
+ * scaled residues run as one element-wise launch before it (two kernel nodes
  * and two memset nodes per graph).
  */
 #ifndef MPRES_GB300_BATCH_H
@@ -64,6 +65,16 @@ int mpres_batch_add_spmv_csrv(mpres_batch_t *batch, int m, const csr_t *csr, con
  * maxnzr column-major slots per row, stored zeros skipped.  The commit reads
  * the slots once to order the rows by length. */
 int mpres_batch_add_spmv_ell(mpres_batch_t *batch, int m, int maxnzr, const ell_t *ell, const void *x, void *y);
+
+/* Same arguments, quick returns and results as mpres_gemm (cuda::mp_gemm,
+ * src/blas/gemm.cuh:69-168): C = alpha*A*B + beta*C, no transposition, one
+ * sequential k chain per output.  The commit sizes a scratch for the operands'
+ * residues scaled by their powers of two ((m*k + k*n) * 4*nmod bytes).  A
+ * batch holding GEMMs runs CTAs of 128 or 256 threads, so its blockDim3 and
+ * threadsPerRow values must not exceed 256. */
+int mpres_batch_add_gemm(mpres_batch_t *batch, int transa, int transb, int m, int n, int k, const mp_array_t *alpha,
+                         const mp_array_t *A, int lda, const mp_array_t *B, int ldb, const mp_array_t *beta,
+                         mp_array_t *C, int ldc);
 
 int mpres_batch_commit(mpres_batch_t *batch, unsigned flags, void *stream);
 int mpres_batch_run(mpres_batch_t *batch, void *stream);

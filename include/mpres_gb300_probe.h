@@ -66,6 +66,16 @@ int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len,
 int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
                          void *stream);
 
+/* The upward fraction sum of the interval evaluation three ways, exact and
+ * bit-identical: which 0 times `count` dependent sums on one warp for each form
+ * (digits = int[32*nmod] residues, result = long long[3] cycles per sum of
+ * {FP64 as the reference, fixed point, integer leaves + FP64 tree}, out =
+ * int[32] checksum); which 1 checks the integer leaves against __dmul_ru /
+ * __dmul_rd on digits = int[count*nmod], result = unsigned long long[4*count*nmod]
+ * {integer RU, __dmul_ru, integer RD, __dmul_rd} bits.  Device memory. */
+int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long count, void *result, int *out,
+                             void *stream);
+
 /* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
  * element per thread: the device functions the BLAS kernels are built from,
  * exposed so that each can be checked against the reference on its own.

@@ -32,6 +32,7 @@
 #include "batch.h"
 #include "kernels.h"
 #include "mp_device.cuh"
+#include "gemm_chain.cuh"
 
 MPRES_DEFINE_TABLES(batch)
 
@@ -41,11 +42,13 @@ struct BatchArgs {
     const GemvOp *gemv;
     const DotOp *dot;
     const SpmvOp *spmv;
+    const GemmOp *gemm;
     const Task *tasks;
     int ntasks;
     int *counters; /* [0] the task counter, [1 + d] finished blocks of DOT d */
     void *buf1;    /* GEMV alpha*x, AoS */
     void *parts;   /* DOT block sums, AoS */
+    const int4 *w; /* GEMM W(A), W(B) */
 };
 
 namespace {
@@ -75,12 +78,22 @@ template <int N> __device__ __forceinline__ void load_aos_cg(mp_t<N> &v, const v
     v.ev[1].exp = __ldcg(p + N / 2 + 4);
 }
 
-/* GEMV buffer1 = alpha * x, one chunk of one operation per block */
+/* The element-wise passes before the persistent kernel, one chunk of one
+ * operation per block: GEMV buffer1 = alpha * x, GEMM W(A) and W(B) */
 template <int N>
-__global__ void __launch_bounds__(256) batch_scale(const GemvOp *ops, const ScaleChunk *chunks, int nchunks,
-                                                   void *buf1) {
+__global__ void __launch_bounds__(256) batch_scale(const GemvOp *ops, const GemmOp *gemms, const ScaleChunk *chunks,
+                                                   int nchunks, void *buf1, int4 *w) {
     for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const ScaleChunk ch = chunks[c];
+        if (ch.kind != kChunkAlphaX) {
+            const GemmOp &g = gemms[ch.op];
+            const long long e = (long long)ch.start + threadIdx.x;
+            if ((int)threadIdx.x < ch.count) {
+                if (ch.kind == kChunkWA) prescale_element<N, true>(g.Ad, g.As, g.Ae, g.lda, g.m, e, w + g.wa);
+                else prescale_element<N, false>(g.Bd, g.Bs, g.Be, g.ldb, g.k, e, w + g.wb);
+            }
+            continue;
+        }
         const GemvOp &g = ops[ch.op];
         const int lx = g.trans ? g.m : g.n;
         const int j = ch.start + (int)threadIdx.x;
@@ -295,7 +308,24 @@ __global__ void ell_row_lengths(const double *as, int m, int maxnzr, int *len) {
     }
 }
 
-template <int N, int MAXT> __global__ void __launch_bounds__(MAXT) batch_kernel(BatchArgs a) {
+/* a 32 x (threads / 32) tile of a GEMM: one output per thread, the lazy-residue
+ * chain of gemm_chain.cuh (the k order is the reference's, so the tile shape
+ * never enters a result) */
+template <int N> __device__ __forceinline__ void gemm_tile(const GemmOp &g, int r0, int c0, const int4 *w) {
+    const int row = r0 + (int)(threadIdx.x & 31), col = c0 + (int)(threadIdx.x >> 5);
+    if (row >= g.m || col >= g.n) return;
+    const MatSoA al{g.ad, g.as, g.ae, g.av, g.alen}, A{g.Ad, g.As, g.Ae, g.Av, g.Alen};
+    const MatSoA B{g.Bd, g.Bs, g.Be, g.Bv, g.Blen}, be{g.bd, g.bs, g.be, g.bv, g.blen};
+    gemm_lazy_output<N>(g.m, g.k, al, A, g.lda, B, g.ldb, be, g.Cd, g.Cs, g.Ce, g.Cv, g.Clen, g.ldc, w + g.wa,
+                        w + g.wb, row, col);
+}
+
+/* The persistent kernel.  Variants with GEMM tiles (GEMM = true) are separate
+ * instantiations: the k chain's registers would otherwise lower the occupancy
+ * of batches without GEMMs.  They exist for 128 threads (three CTAs an SM, as
+ * the plain GEMM kernel) and 256. */
+template <int N, int MAXT, bool GEMM>
+__global__ void __launch_bounds__(MAXT, (GEMM && MAXT == 128) ? 3 : 1) batch_kernel(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     mp_t<N> *sdata = reinterpret_cast<mp_t<N> *>(smem);
     __shared__ int s_task, s_flag;
@@ -307,8 +337,29 @@ template <int N, int MAXT> __global__ void __launch_bounds__(MAXT) batch_kernel(
         const Task tk = a.tasks[ti];
         if (tk.kind == kGemvTile) gemv_tile<N>(a.gemv[tk.op], tk.a, a.buf1, sdata);
         else if (tk.kind == kDotGroup) dot_group<N>(a.dot[tk.op], tk.op, tk.a, tk.b, a.parts, a.counters + 1, sdata, &s_flag);
+        else if (GEMM && tk.kind == kGemmTile) gemm_tile<N>(a.gemm[tk.op], tk.a, tk.b, a.w);
         else spmv_chunk<N>(a.spmv[tk.op], tk.a, tk.b);
         __syncthreads();
+    }
+}
+
+/* snapshot / restore of every GEMM output C (column-major, ldc), for autotuning */
+template <int N> __global__ void gemm_c_copy(const GemmOp *ops, int nops, const long long *offs, void *save, int dir) {
+    const int op = blockIdx.y;
+    if (op >= nops) return;
+    const GemmOp &g = ops[op];
+    const long long outs = (long long)g.m * g.n;
+    const int lenc = __ldg(g.Clen);
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < outs; o += (long long)gridDim.x * blockDim.x) {
+        const long long ic = (o / g.m) * g.ldc + o % g.m;
+        mp_t<N> v;
+        if (dir == 0) {
+            load_soa<N>(v, g.Cd, g.Cs, g.Ce, g.Cv, lenc, ic);
+            store_aos<N>(v, save, offs[op] + o);
+        } else {
+            load_aos<N>(v, save, offs[op] + o);
+            store_soa<N>(v, g.Cd, g.Cs, g.Ce, g.Cv, lenc, ic);
+        }
     }
 }
 
@@ -352,21 +403,29 @@ int shape_slot(int nmod) {
 }
 
 /* the kernel's shared-memory limit, raised on each device that runs a variant */
-template <int N, int MAXT> cudaError_t set_attr() {
+template <int N, int MAXT, bool GEMM> cudaError_t set_attr() {
     static PerDevice<cudaError_t> attrs(cuda_ok);
     return attrs.get(current_device(), cudaErrorInvalidDevice, [] {
-        return cudaFuncSetAttribute(batch_kernel<N, MAXT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        return cudaFuncSetAttribute(batch_kernel<N, MAXT, GEMM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     MAXT * (int)sizeof(mp_t<N>));
     });
 }
 
-template <int N, int MAXT> int occupancy(int threads) {
+template <int N, int MAXT, bool GEMM> int occupancy(int threads) {
     int per_sm = 0;
-    if (set_attr<N, MAXT>() != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<N, MAXT>, threads,
+    if (set_attr<N, MAXT, GEMM>() != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<N, MAXT, GEMM>, threads,
                                                       (size_t)threads * sizeof(mp_t<N>)) != cudaSuccess)
         return 0;
     return per_sm;
+}
+
+template <int N, int MAXT, bool GEMM>
+cudaError_t launch_variant(const BatchArgs &a, int threads, int ctas, cudaStream_t s) {
+    cudaError_t e = set_attr<N, MAXT, GEMM>();
+    if (e != cudaSuccess) return e;
+    batch_kernel<N, MAXT, GEMM><<<ctas, threads, (size_t)threads * sizeof(mp_t<N>), s>>>(a);
+    return cudaGetLastError();
 }
 
 template <int N>
@@ -375,25 +434,23 @@ cudaError_t launch_n(const BatchHost &b, const BatchDev &d, int threads, int cta
     if (e != cudaSuccess) return e;
     if (!b.chunks.empty()) {
         const int g = (int)std::min<size_t>(b.chunks.size(), 152 * 16);
-        batch_scale<N><<<g, 256, 0, s>>>(d.gemv, d.chunks, (int)b.chunks.size(), d.buf1);
+        batch_scale<N><<<g, 256, 0, s>>>(d.gemv, d.gemm, d.chunks, (int)b.chunks.size(), d.buf1,
+                                         static_cast<int4 *>(d.w));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if (b.tasks.empty()) return cudaSuccess;
-    BatchArgs a{d.gemv, d.dot, d.spmv, d.tasks, (int)b.tasks.size(), d.counters, d.buf1, d.parts};
-    const size_t smem = (size_t)threads * sizeof(mp_t<N>);
-    /* register budgets: 256-thread CTAs may use up to 255 registers a thread,
-     * 512 up to 128, 1024 up to 64 */
-    if (threads <= 256) {
-        if ((e = set_attr<N, 256>()) != cudaSuccess) return e;
-        batch_kernel<N, 256><<<ctas, threads, smem, s>>>(a);
-    } else if (threads <= 512) {
-        if ((e = set_attr<N, 512>()) != cudaSuccess) return e;
-        batch_kernel<N, 512><<<ctas, threads, smem, s>>>(a);
-    } else {
-        if ((e = set_attr<N, 1024>()) != cudaSuccess) return e;
-        batch_kernel<N, 1024><<<ctas, threads, smem, s>>>(a);
+    BatchArgs a{d.gemv, d.dot, d.spmv, d.gemm, d.tasks, (int)b.tasks.size(), d.counters, d.buf1, d.parts,
+                static_cast<const int4 *>(d.w)};
+    /* register budgets: 128-thread GEMM CTAs up to 168 registers a thread,
+     * 256-thread CTAs up to 255, 512 up to 128, 1024 up to 64 */
+    if (!b.gemm.empty()) {
+        if (threads <= 128) return launch_variant<N, 128, true>(a, threads, ctas, s);
+        if (threads <= 256) return launch_variant<N, 256, true>(a, threads, ctas, s);
+        return cudaErrorInvalidConfiguration;
     }
-    return cudaGetLastError();
+    if (threads <= 256) return launch_variant<N, 256, false>(a, threads, ctas, s);
+    if (threads <= 512) return launch_variant<N, 512, false>(a, threads, ctas, s);
+    return launch_variant<N, 1024, false>(a, threads, ctas, s);
 }
 
 template <class T> size_t bytes_of(const std::vector<T> &v) { return sizeof(T) * v.size(); }
@@ -454,6 +511,27 @@ void batch_add_spmv_ell(BatchHost &b, int m, int maxnzr, const ell_t &ell, const
     b.spmv_len.push_back({});
 }
 
+bool batch_add_gemm(BatchHost &b, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
+                    const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc, int nmod) {
+    /* the quick returns of src/blas/gemm.cuh:77-96 (no transposition) */
+    if (m <= 0 || n <= 0 || k <= 0 || lda < (m > 1 ? m : 1) || ldb < (k > 1 ? k : 1) || ldc < (m > 1 ? m : 1))
+        return false;
+    GemmOp g{};
+    g.ad = alpha.digits; g.as = alpha.sign; g.ae = alpha.exp; g.av = ev(alpha); g.alen = alpha.len;
+    g.Ad = A.digits; g.As = A.sign; g.Ae = A.exp; g.Av = ev(A); g.Alen = A.len;
+    g.Bd = B.digits; g.Bs = B.sign; g.Be = B.exp; g.Bv = ev(B); g.Blen = B.len;
+    g.bd = beta.digits; g.bs = beta.sign; g.be = beta.exp; g.bv = ev(beta); g.blen = beta.len;
+    g.Cd = C.digits; g.Cs = C.sign; g.Ce = C.exp; g.Cv = ev(C); g.Clen = C.len;
+    g.m = m; g.n = n; g.k = k; g.lda = lda; g.ldb = ldb; g.ldc = ldc;
+    const long long q = nmod / 4;
+    g.wa = b.w_elems;
+    b.w_elems += (long long)m * k * q;
+    g.wb = b.w_elems;
+    b.w_elems += (long long)k * n * q;
+    b.gemm.push_back(g);
+    return true;
+}
+
 void spmv_row_order(const int *irp, int m, std::vector<int> &order, std::vector<int> &lens) {
     /* counting sort by length, longest first, rows of equal length in order */
     int maxlen = 0;
@@ -482,7 +560,7 @@ bool batch_plan(BatchHost &b, int threads) {
         /* chain length in multiply-add steps, plus the tree */
         const long long cost = (inner + g.b3 - 1) / g.b3 + 2 * (32 - __builtin_clz((unsigned)g.b3));
         for (int o = 0; o < outs; o += g.R) items.push_back({cost, {kGemvTile, (int)i, o, 0}});
-        for (int j = 0; j < inner; j += 256) b.chunks.push_back({(int)i, j, std::min(256, inner - j), 0});
+        for (int j = 0; j < inner; j += 256) b.chunks.push_back({(int)i, j, std::min(256, inner - j), kChunkAlphaX});
     }
     for (size_t i = 0; i < b.dot.size(); i++) {
         DotOp &d = b.dot[i];
@@ -505,6 +583,20 @@ bool batch_plan(BatchHost &b, int threads) {
             items.push_back({cost, {kSpmvChunk, (int)i, r, std::min(rows, sp.m - r)}});
         }
     }
+    for (size_t i = 0; i < b.gemm.size(); i++) {
+        const GemmOp &g = b.gemm[i];
+        if (threads > 256) return false;
+        const int cols = threads / 32;
+        /* cost in chain steps: the k chain, then the epilogue's products and addition */
+        const long long cost = g.k + 8;
+        for (int r = 0; r < g.m; r += 32)
+            for (int c = 0; c < g.n; c += cols) items.push_back({cost, {kGemmTile, (int)i, r, c}});
+        const long long na = (long long)g.m * g.k, nb = (long long)g.k * g.n;
+        for (long long e = 0; e < na; e += 256)
+            b.chunks.push_back({(int)i, (int)e, (int)std::min<long long>(256, na - e), kChunkWA});
+        for (long long e = 0; e < nb; e += 256)
+            b.chunks.push_back({(int)i, (int)e, (int)std::min<long long>(256, nb - e), kChunkWB});
+    }
     std::stable_sort(items.begin(), items.end(), [](const Item &x, const Item &y) { return x.cost > y.cost; });
     b.tasks.resize(items.size());
     for (size_t i = 0; i < items.size(); i++) b.tasks[i] = items[i].t;
@@ -516,7 +608,8 @@ TableLayout batch_layout(const BatchHost &b) {
     l.gemv = 0;
     l.dot = align256(l.gemv + bytes_of(b.gemv));
     l.spmv = align256(l.dot + bytes_of(b.dot));
-    l.tasks = align256(l.spmv + bytes_of(b.spmv));
+    l.gemm = align256(l.spmv + bytes_of(b.spmv));
+    l.tasks = align256(l.gemm + bytes_of(b.gemm));
     l.chunks = align256(l.tasks + bytes_of(b.tasks));
     l.counters = align256(l.chunks + bytes_of(b.chunks));
     l.total = align256(l.counters + sizeof(int) * (1 + b.dot.size()));
@@ -528,17 +621,20 @@ void batch_pack(const BatchHost &b, const TableLayout &l, void *host_buf) {
     if (!b.gemv.empty()) std::memcpy(p + l.gemv, b.gemv.data(), bytes_of(b.gemv));
     if (!b.dot.empty()) std::memcpy(p + l.dot, b.dot.data(), bytes_of(b.dot));
     if (!b.spmv.empty()) std::memcpy(p + l.spmv, b.spmv.data(), bytes_of(b.spmv));
+    if (!b.gemm.empty()) std::memcpy(p + l.gemm, b.gemm.data(), bytes_of(b.gemm));
     if (!b.tasks.empty()) std::memcpy(p + l.tasks, b.tasks.data(), bytes_of(b.tasks));
     if (!b.chunks.empty()) std::memcpy(p + l.chunks, b.chunks.data(), bytes_of(b.chunks));
 }
 
-BatchDev batch_dev_at(const BatchHost &b, const TableLayout &l, void *dev_buf, void *buf1, void *parts) {
+BatchDev batch_dev_at(const BatchHost &b, const TableLayout &l, void *dev_buf, void *buf1, void *parts, void *w) {
     (void)b;
     char *p = static_cast<char *>(dev_buf);
     BatchDev d;
     d.gemv = reinterpret_cast<GemvOp *>(p + l.gemv);
     d.dot = reinterpret_cast<DotOp *>(p + l.dot);
     d.spmv = reinterpret_cast<SpmvOp *>(p + l.spmv);
+    d.gemm = reinterpret_cast<GemmOp *>(p + l.gemm);
+    d.w = w;
     d.tasks = reinterpret_cast<Task *>(p + l.tasks);
     d.chunks = reinterpret_cast<ScaleChunk *>(p + l.chunks);
     d.counters = reinterpret_cast<int *>(p + l.counters);
@@ -556,14 +652,17 @@ cudaError_t batch_launch(int nmod, const BatchHost &b, const BatchDev &d, int th
     }
 }
 
-int batch_ctas_per_sm(int nmod, int threads) {
-#define MPRES_OCC(NN)                                                                               \
-    return threads <= 256 ? occupancy<NN, 256>(threads)                                             \
-                          : (threads <= 512 ? occupancy<NN, 512>(threads) : occupancy<NN, 1024>(threads))
-    if (nmod == 8) MPRES_OCC(8);
-    if (nmod == 16) MPRES_OCC(16);
-    if (nmod == 32) MPRES_OCC(32);
-#undef MPRES_OCC
+template <int N> int ctas_per_sm_n(int threads, bool gemm) {
+    if (gemm) return threads <= 128 ? occupancy<N, 128, true>(threads)
+                                    : (threads <= 256 ? occupancy<N, 256, true>(threads) : 0);
+    return threads <= 256 ? occupancy<N, 256, false>(threads)
+                          : (threads <= 512 ? occupancy<N, 512, false>(threads) : occupancy<N, 1024, false>(threads));
+}
+
+int batch_ctas_per_sm(int nmod, int threads, bool gemm) {
+    if (nmod == 8) return ctas_per_sm_n<8>(threads, gemm);
+    if (nmod == 16) return ctas_per_sm_n<16>(threads, gemm);
+    if (nmod == 32) return ctas_per_sm_n<32>(threads, gemm);
     return 0;
 }
 
@@ -581,19 +680,35 @@ static void cache_shape(int nmod, int threads, int per_sm) {
     g_shape_cache[shape_slot(nmod)] = {threads, per_sm};
 }
 
-/* snapshot (dir 0) or restore (dir 1) of every GEMV output of a batch */
+/* snapshot (dir 0) or restore (dir 1) of every output a run accumulates into
+ * (GEMV y, GEMM C): offs[op] for the GEMVs, then for the GEMMs */
 static cudaError_t gemv_outputs(int nmod, const BatchHost &b, const BatchDev &d, const long long *offs, void *save,
                                 int dir, cudaStream_t s) {
-    if (b.gemv.empty()) return cudaSuccess;
-    dim3 grid(8, (unsigned)b.gemv.size());
-    const int nops = (int)b.gemv.size();
-    switch (nmod) {
-    case 8: gemv_y_copy<8><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
-    case 16: gemv_y_copy<16><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
-    case 32: gemv_y_copy<32><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
-    default: return cudaErrorInvalidValue;
+    if (!b.gemv.empty()) {
+        dim3 grid(8, (unsigned)b.gemv.size());
+        const int nops = (int)b.gemv.size();
+        switch (nmod) {
+        case 8: gemv_y_copy<8><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
+        case 16: gemv_y_copy<16><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
+        case 32: gemv_y_copy<32><<<grid, 256, 0, s>>>(d.gemv, nops, offs, save, dir); break;
+        default: return cudaErrorInvalidValue;
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
     }
-    return cudaGetLastError();
+    if (!b.gemm.empty()) {
+        dim3 grid(64, (unsigned)b.gemm.size());
+        const int nops = (int)b.gemm.size();
+        const long long *go = offs + b.gemv.size();
+        switch (nmod) {
+        case 8: gemm_c_copy<8><<<grid, 256, 0, s>>>(d.gemm, nops, go, save, dir); break;
+        case 16: gemm_c_copy<16><<<grid, 256, 0, s>>>(d.gemm, nops, go, save, dir); break;
+        case 32: gemm_c_copy<32><<<grid, 256, 0, s>>>(d.gemm, nops, go, save, dir); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
 }
 
 } // namespace mpres
@@ -607,7 +722,7 @@ struct mpres_batch {
     bool committed = false;
     BatchHost host;
     void *tables = nullptr; /* device tables (batch_layout) */
-    void *buf1 = nullptr, *parts = nullptr;
+    void *buf1 = nullptr, *parts = nullptr, *w = nullptr;
     int *perm = nullptr;
     BatchDev dev;
     int threads = 256, ctas = 0, candidates = 0;
@@ -617,9 +732,9 @@ struct mpres_batch {
 };
 
 static void release(mpres_batch *b) {
-    for (void *p : {b->tables, b->buf1, b->parts, (void *)b->perm})
+    for (void *p : {b->tables, b->buf1, b->parts, b->w, (void *)b->perm})
         if (p) cudaFree(p);
-    b->tables = b->buf1 = b->parts = nullptr;
+    b->tables = b->buf1 = b->parts = b->w = nullptr;
     b->perm = nullptr;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
@@ -642,7 +757,7 @@ static cudaError_t plan_and_upload(mpres_batch *b, int threads, size_t &cap) {
     std::vector<char> staging(l.total);
     batch_pack(b->host, l, staging.data());
     if ((e = cudaMemcpy(b->tables, staging.data(), l.total, cudaMemcpyHostToDevice)) != cudaSuccess) return e;
-    b->dev = batch_dev_at(b->host, l, b->tables, b->buf1, b->parts);
+    b->dev = batch_dev_at(b->host, l, b->tables, b->buf1, b->parts, b->w);
     return cudaSuccess;
 }
 
@@ -723,6 +838,20 @@ int mpres_batch_add_spmv_ell(mpres_batch_t *b, int m, int maxnzr, const ell_t *e
     return status_ok();
 }
 
+int mpres_batch_add_gemm(mpres_batch_t *b, int transa, int transb, int m, int n, int k, const mp_array_t *alpha,
+                         const mp_array_t *A, int lda, const mp_array_t *B, int ldb, const mp_array_t *beta,
+                         mp_array_t *C, int ldc) {
+    if (int st = check_open(b, "mpres_batch_add_gemm")) return st;
+    if (m <= 0 || n <= 0 || k <= 0) return status_ok();
+    if (transa != MPRES_NO_TRANS || transb != MPRES_NO_TRANS)
+        return status_fail(MPRES_ERR_NOT_SUPPORTED, "mpres_batch_add_gemm: only non-transposed matrices are supported");
+    if (!alpha || !A || !B || !beta || !C) return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_batch_add_gemm: null array");
+    if ((long long)m * k >= (1ll << 31) || (long long)k * n >= (1ll << 31))
+        return status_fail(MPRES_ERR_NOT_SUPPORTED, "mpres_batch_add_gemm: m*k and k*n must stay below 2^31");
+    batch_add_gemm(b->host, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, b->nmod);
+    return status_ok();
+}
+
 int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
     if (int st = check_open(b, "mpres_batch_commit")) return st;
     int dev = 0;
@@ -772,6 +901,9 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
         return status_cuda(e, "mpres_batch_commit (alpha*x)");
     if (h.part_elems && (e = cudaMalloc(&b->parts, rec * h.part_elems)) != cudaSuccess)
         return status_cuda(e, "mpres_batch_commit (block sums)");
+    if (h.w_elems && (e = cudaMalloc(&b->w, sizeof(int4) * (size_t)h.w_elems)) != cudaSuccess)
+        return status_cuda(e, "mpres_batch_commit (GEMM W(A), W(B))");
+    const bool gemm = !h.gemm.empty();
     /* launch shape: the largest blockDim3 (or threadsPerRow) is the least threads per CTA */
     int min_threads = 32;
     for (const GemvOp &g : h.gemv) min_threads = std::max(min_threads, g.b3);
@@ -781,21 +913,25 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     std::vector<std::pair<int, int>> cand; /* threads, CTAs per SM */
     int ct = 0, cp = 0;
+    /* batches with GEMM tiles run 128 or 256 threads per CTA */
+    if (gemm && min_threads > 256)
+        return status_fail(MPRES_ERR_NOT_SUPPORTED,
+                           "mpres_batch_commit: a batch with GEMMs takes blockDim3 and threadsPerRow <= 256");
     if (flags & MPRES_BATCH_AUTOTUNE) {
         for (int t : {128, 256, 512, 1024}) {
-            if (t < min_threads) continue;
-            const int occ = batch_ctas_per_sm(b->nmod, t);
+            if (t < min_threads || (gemm && t > 256)) continue;
+            const int occ = batch_ctas_per_sm(b->nmod, t, gemm);
             for (int p : {1, 2, 4, occ})
                 if (p >= 1 && p <= occ && std::find(cand.begin(), cand.end(), std::make_pair(t, p)) == cand.end())
                     cand.push_back({t, p});
         }
-    } else if (batch_cached_shape(b->nmod, ct, cp) && ct >= min_threads) {
+    } else if (!gemm && batch_cached_shape(b->nmod, ct, cp) && ct >= min_threads) {
         cand.push_back({ct, cp});
     }
     if (cand.empty()) {
-        int t = 256;
+        int t = gemm ? 128 : 256;
         while (t < min_threads) t *= 2;
-        const int occ = batch_ctas_per_sm(b->nmod, t);
+        const int occ = batch_ctas_per_sm(b->nmod, t, gemm);
         if (occ < 1) return status_fail(MPRES_ERR_NOT_SUPPORTED, "mpres_batch_commit: no launch shape fits");
         cand.push_back({t, occ});
     }
@@ -808,6 +944,10 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
         for (const GemvOp &g : h.gemv) {
             offs.push_back(outs_total);
             outs_total += g.trans ? g.n : g.m;
+        }
+        for (const GemmOp &g : h.gemm) {
+            offs.push_back(outs_total);
+            outs_total += (long long)g.m * g.n;
         }
         void *save = nullptr;
         long long *d_offs = nullptr;
@@ -853,13 +993,13 @@ int mpres_batch_commit(mpres_batch_t *b, unsigned flags, void *stream) {
         if (d_offs) cudaFree(d_offs);
         if (e != cudaSuccess) return status_cuda(e, "mpres_batch_commit (autotune)");
         b->autotuned = true;
-        cache_shape(b->nmod, cand[best].first, cand[best].second);
+        if (!gemm) cache_shape(b->nmod, cand[best].first, cand[best].second);
     }
     b->candidates = cand.size() > 1 ? (int)cand.size() : 0;
     b->threads = cand[best].first;
     b->ctas = cand[best].second * sms;
     if ((e = plan_and_upload(b, b->threads, cap)) != cudaSuccess) return status_cuda(e, "mpres_batch_commit (tables)");
-    batch_ctas_per_sm(b->nmod, b->threads); /* raises the shared-memory limit before any capture */
+    batch_ctas_per_sm(b->nmod, b->threads, gemm); /* raises the shared-memory limit before any capture */
     if (flags & MPRES_BATCH_GRAPH) {
         cudaStream_t cs;
         if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)
@@ -890,13 +1030,13 @@ int mpres_batch_info(const mpres_batch_t *b, long long *out) {
     if (!b || !out) return status_fail(MPRES_ERR_INVALID_VALUE, "mpres_batch_info: null argument");
     const size_t rec = 4 * (size_t)b->nmod + 40;
     const BatchHost &h = b->host;
-    out[0] = (long long)(h.gemv.size() + h.dot.size() + h.spmv.size());
+    out[0] = (long long)(h.gemv.size() + h.dot.size() + h.spmv.size() + h.gemm.size());
     out[1] = (long long)h.tasks.size();
     out[2] = b->threads;
     out[3] = b->ctas;
     out[4] = b->exec != nullptr;
     out[5] = b->autotuned;
-    out[6] = (long long)(rec * (h.buf1_elems + h.part_elems));
+    out[6] = (long long)(rec * (h.buf1_elems + h.part_elems) + sizeof(int4) * h.w_elems);
     out[7] = b->candidates;
     return status_ok();
 }

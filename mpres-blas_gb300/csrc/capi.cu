@@ -792,6 +792,15 @@ int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int cou
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_rounding");
 }
 
+int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long count, void *result, int *out,
+                             void *stream) {
+    if (int st = require(nmod)) return st;
+    if ((which != 0 && which != 1) || count <= 0 || !digits || !result || (which == 0 && !out))
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_fraction_sum: bad arguments");
+    cudaError_t e = launch_psum_probe(nmod, which, digits, count, result, out, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_fraction_sum");
+}
+
 int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {
     if (int st = require(nmod)) return st;
     if (count == 0) return ok();

@@ -139,10 +139,107 @@ __global__ void round_parts_probe(const int *digits, const unsigned *D, int coun
     out[lane] = acc;
 }
 
+/* The upward leaf RU(s * recip_ru_i) of the fraction sums, exactly, on the
+ * integer pipes: recip_ru_i = R * 2^-83 with a 53-bit R, so s * recip_ru_i is
+ * the 84-bit integer P = s * R times 2^-83; rounding it up to 53 significant
+ * bits and assembling the double's fields gives the same double __dmul_ru
+ * gives (UP = false: truncation, __dmul_rd with recip_rd_i). */
+template <int N, bool UP> __device__ __forceinline__ double int_leaf(uint32_t s, int i) {
+    const Tables<N> &t = T<N>();
+    const uint64_t R = UP ? t.recip_ru_m[i] : t.recip_rd_m[i];
+    const uint64_t lo = (uint64_t)s * (uint32_t)R, hi = (uint64_t)s * (uint32_t)(R >> 32);
+    const uint64_t plo = lo + (hi << 32);
+    const uint64_t phi = (hi >> 32) + (plo < lo);
+    if ((plo | phi) == 0) return 0.0;
+    const int L = phi ? 128 - __clzll((long long)phi) : 64 - __clzll((long long)plo);
+    uint64_t q;
+    bool sticky;
+    if (L > 53) {
+        const int sh = L - 53; /* 1 .. 31 */
+        q = (plo >> sh) | (phi << (64 - sh));
+        sticky = (plo << (64 - sh)) != 0;
+    } else {
+        q = plo << (53 - L);
+        sticky = false;
+    }
+    int e = L - 1 - 83; /* the value is in [2^e, 2^(e+1)) */
+    if (UP && sticky) {
+        q++;
+        if (q >> 53) {
+            q >>= 1;
+            e++;
+        }
+    }
+    return bdbl(((uint64_t)(e + 1023) << 52) | (q & ((1ull << 52) - 1)));
+}
+
+/* cycles of `reps` dependent fraction sums: form 0 = FP64 (the kernels' psum),
+ * 1 = fixed point (fixed_eval.cuh), 2 = integer leaves and the FP64 tree */
+template <int N>
+__global__ void psum_probe(const int *digits, int form, int reps, long long *cycles, int *out) {
+    const Tables<N> &t = T<N>();
+    const int lane = threadIdx.x;
+    int s[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) s[i] = __ldg(digits + lane * N + i);
+    int acc = 0;
+    __syncwarp();
+    const long long t0 = clock64();
+    for (int r = 0; r < reps; r++) {
+        uint64_t bits;
+        if (form == 0) {
+            bits = dbits(psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); }));
+        } else if (form == 1) {
+            const fx f = fx_fraction_sum<N, true>(s);
+            bits = f.lo ^ f.hi;
+        } else {
+            bits = dbits(psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); }));
+        }
+        s[0] ^= (int)(bits & 1); /* the next sum depends on this one */
+        acc += (int)(bits >> 20);
+    }
+    const long long t1 = clock64();
+    if (lane == 0) cycles[form] = (t1 - t0) / reps;
+    out[lane] = acc + s[0];
+}
+
+/* int_leaf against __dmul_ru / __dmul_rd: out[4*i..] = {int RU, dmul RU, int RD, dmul RD} bits */
+template <int N> __global__ void int_leaf_check(const int *digits, long long count, unsigned long long *out) {
+    const Tables<N> &t = T<N>();
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < count * N;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % N);
+        const uint32_t s = (uint32_t)__ldg(digits + e);
+        out[4 * e] = dbits(int_leaf<N, true>(s, i));
+        out[4 * e + 1] = dbits(__dmul_ru(u31_to_double(s), t.recip_ru[i]));
+        out[4 * e + 2] = dbits(int_leaf<N, false>(s, i));
+        out[4 * e + 3] = dbits(__dmul_rd(u31_to_double(s), t.recip_rd[i]));
+    }
+}
+
 } // namespace chainprobe
 } // namespace mpres
 
 /* the host launchers of this translation unit's instantiations */
+#define MPRES_PSUM_PROBE_LAUNCHER(NAME)                                                                        \
+    cudaError_t NAME(int nmod, int which, const int *digits, long long count, void *cycles_or_out, int *out,  \
+                     cudaStream_t s) {                                                                          \
+        if (which == 0) {                                                                                      \
+            for (int f = 0; f < 3; f++) {                                                                      \
+                if (nmod == 8) chainprobe::psum_probe<8><<<1, 32, 0, s>>>(digits, f, (int)count, (long long *)cycles_or_out, out); \
+                else if (nmod == 16) chainprobe::psum_probe<16><<<1, 32, 0, s>>>(digits, f, (int)count, (long long *)cycles_or_out, out); \
+                else if (nmod == 32) chainprobe::psum_probe<32><<<1, 32, 0, s>>>(digits, f, (int)count, (long long *)cycles_or_out, out); \
+                else return cudaErrorInvalidValue;                                                             \
+            }                                                                                                  \
+            return cudaGetLastError();                                                                         \
+        }                                                                                                      \
+        const int g = 512;                                                                                     \
+        if (nmod == 8) chainprobe::int_leaf_check<8><<<g, 256, 0, s>>>(digits, count, (unsigned long long *)cycles_or_out); \
+        else if (nmod == 16) chainprobe::int_leaf_check<16><<<g, 256, 0, s>>>(digits, count, (unsigned long long *)cycles_or_out); \
+        else if (nmod == 32) chainprobe::int_leaf_check<32><<<g, 256, 0, s>>>(digits, count, (unsigned long long *)cycles_or_out); \
+        else return cudaErrorInvalidValue;                                                                     \
+        return cudaGetLastError();                                                                             \
+    }
 #define MPRES_ROUND_PROBE_LAUNCHER(NAME)                                                                      \
     cudaError_t NAME(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,  \
                      cudaStream_t s) {                                                                        \

@@ -546,19 +546,26 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
 #endif
 }
 
-/* The rank of a number -- floor(V) for V = sum_i s_i / m_i -- the way the
- * reference obtains it: the whole parts of the directed-rounding pairwise sums
- * of the leaves RD/RU(s_i * recip_i) (rank_full compares both, rank_fast takes
- * the upward one).  Those sums bracket V within 2^-42: each of the N <= 32
- * leaves is below 1 and errs by less than 2^-53, each of the N - 1 additions
- * of partial sums below 32 by less than 2^-48.  So whenever frac(V) lies in
- * [2^-40, 1 - 2^-40] both whole parts equal floor(V), and floor(V) is the
- * rank exactly.  rank_shortcut decides that from the exact integer sum
- * S = sum_i s_i * floor(2^94 / m_i) (V - 2^-58 < S / 2^94 <= V): it returns
- * true with floor(V) in `rank` when the top 42 fraction bits of S keep a
- * margin of 2^-39 from both integers, and false otherwise -- then the FP64
- * sums decide, as in the reference.  Integer pipes only, about 40 instructions
- * instead of one or two 2N-1-operation FP64 sums. */
+/* The rank of a number X -- floor(V) for V = sum_i s_i / m_i, where
+ * V = rank + X/M -- the way the reference obtains it: the whole parts whl, whu
+ * of the directed-rounding pairwise sums PD <= V <= PU of the leaves
+ * RD/RU(s_i * recip_i); rank_fast takes whu, rank_full takes whl if whl == whu
+ * and otherwise whu when the top mixed-radix digit mrd(x) is 0, whl when not.
+ * The sums bracket V within 2^-41.9 (each of the N <= 32 leaves errs by less
+ * than 2^-51, each of the N - 1 additions of partial sums below 32 by less
+ * than 2^-47), so whenever frac(V) <= 1 - 2^-40:
+ *   whu = floor(V), as PU < V + 2^-41.9 < floor(V) + 1;
+ *   whl = floor(V) when frac(V) >= 2^-40, and otherwise whl is floor(V) or
+ *   floor(V) - 1; in that case X/M = frac(V) < 2^-40 < 1 / m_(N-1), so X is
+ *   below the product of the other moduli, mrd(x) = 0, and rank_full returns
+ *   whu = floor(V) as well.
+ * Both ranks are floor(V) then.  rank_shortcut decides it from the exact
+ * integer sum S = sum_i s_i * floor(2^94 / m_i), V - 2^-58 < S / 2^94 <= V:
+ * when the top 42 fraction bits of S stay 2^-39 below the next integer it
+ * returns true with floor(V) = floor(S / 2^94) in `rank`; otherwise (frac(V)
+ * just below an integer) the FP64 sums decide, as in the reference.  In a
+ * rounding X/M is tiny, so the shortcut holds; it costs about 40 integer
+ * instructions instead of one or two 2N-1-operation FP64 sums. */
 template <int N> __device__ __forceinline__ bool rank_shortcut(const int *s, unsigned int &rank) {
     const Tables<N> &t = T<N>();
     unsigned __int128 S = 0;
@@ -566,7 +573,7 @@ template <int N> __device__ __forceinline__ bool rank_shortcut(const int *s, uns
     for (int i = 0; i < N; i++) S += (unsigned __int128)(uint32_t)s[i] * t.inv94[i];
     const uint64_t top = (uint64_t)(S >> 52) & ((1ull << 42) - 1); /* fraction bits 2^-1 .. 2^-42 */
     rank = (unsigned int)(S >> 94);
-    return top >= 8 && top <= (1ull << 42) - 9;
+    return top <= (1ull << 42) - 9;
 }
 
 /* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */

@@ -261,7 +261,7 @@ bool launch(mpres_server *s, Slot &sl, std::vector<Req> &reqs, cudaError_t &err)
     batch_pack(h, l, sl.staging);
     char *sbase = s->arena.at(off);
     const BatchDev d = batch_dev_at(h, l, sl.tables, buf1 ? sbase : nullptr,
-                                    parts ? sbase + ((buf1 + 255) & ~(size_t)255) : nullptr);
+                                    parts ? sbase + ((buf1 + 255) & ~(size_t)255) : nullptr, nullptr);
     err = cudaMemcpyAsync(sl.tables, sl.staging, l.total, cudaMemcpyHostToDevice, sl.stream);
     if (err == cudaSuccess) err = batch_launch(s->nmod, h, d, threads, per_sm * s->sms, sl.stream);
     if (err == cudaSuccess) err = cudaEventRecord(sl.done, sl.stream);

@@ -89,6 +89,7 @@ _SIGS = {
     "mpres_batch_add_spmv_csr": (I, [P, I, P, P, P]),
     "mpres_batch_add_spmv_csrv": (I, [P, I, P, P, P, I]),
     "mpres_batch_add_spmv_ell": (I, [P, I, I, P, P, P]),
+    "mpres_batch_add_gemm": (I, [P, I, I, I, I, I, P, P, I, P, I, P, P, I]),
     "mpres_batch_commit": (I, [P, ctypes.c_uint, P]),
     "mpres_batch_run": (I, [P, P]),
     "mpres_batch_info": (I, [P, P]),
@@ -110,6 +111,7 @@ _SIGS = {
     "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_chain": (I, [I, I, P, P, I, P, P, P, P]),
     "mpres_probe_rounding": (I, [I, P, P, I, P, P, P]),
+    "mpres_probe_fraction_sum": (I, [I, I, P, ctypes.c_longlong, P, P, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
     "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
 }
@@ -566,6 +568,11 @@ class Batch:
         check(lib().mpres_batch_add_spmv_csr(self.h, m, ctypes.byref(csr.c), x.ptr, y.ptr),
               "mpres_batch_add_spmv_csr")
 
+    def add_gemm(self, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, transa=NO_TRANS, transb=NO_TRANS):
+        self._keep += [alpha, A, B, beta, C]
+        check(lib().mpres_batch_add_gemm(self.h, transa, transb, m, n, k, alpha.ref, A.ref, lda, B.ref, ldb, beta.ref,
+                                         C.ref, ldc), "mpres_batch_add_gemm")
+
     def add_spmv_csrv(self, m, csr, x, y, tpr):
         self._keep += [csr, x, y]
         check(lib().mpres_batch_add_spmv_csrv(self.h, m, ctypes.byref(csr.c), x.ptr, y.ptr, tpr),
@@ -749,6 +756,27 @@ def probe_rounding(nmod, digits, D, count):
     check(lib().mpres_probe_rounding(nmod, dd.ptr, dD.ptr, count, cyc.ptr, out.ptr, None), "mpres_probe_rounding")
     torch.cuda.synchronize()
     return cyc.to_numpy(np.int64, 5 * count).reshape(count, 5)
+
+
+def probe_fraction_sum_cycles(nmod, digits, reps=64):
+    """Cycles per upward fraction sum on one warp: {FP64, fixed point, integer leaves + FP64 tree}."""
+    import torch
+    dd = DeviceBytes.from_numpy(np.ascontiguousarray(digits, dtype=np.int32))
+    cyc, out = DeviceBytes(8 * 3), DeviceBytes(4 * 32)
+    check(lib().mpres_probe_fraction_sum(nmod, 0, dd.ptr, reps, cyc.ptr, out.ptr, None), "mpres_probe_fraction_sum")
+    torch.cuda.synchronize()
+    return cyc.to_numpy(np.int64, 3)
+
+
+def probe_int_leaves(nmod, digits):
+    """{integer RU, __dmul_ru, integer RD, __dmul_rd} leaf bits per residue (mpres_probe_fraction_sum)."""
+    import torch
+    digits = np.ascontiguousarray(digits, dtype=np.int32)
+    count = digits.size // nmod
+    dd, res = DeviceBytes.from_numpy(digits), DeviceBytes(8 * 4 * digits.size)
+    check(lib().mpres_probe_fraction_sum(nmod, 1, dd.ptr, count, res.ptr, None, None), "mpres_probe_fraction_sum")
+    torch.cuda.synchronize()
+    return res.to_numpy(np.uint64, 4 * digits.size).reshape(-1, 4)
 
 
 def probe_check(which, nmod, a, b=None):

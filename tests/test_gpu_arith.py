@@ -180,3 +180,19 @@ def test_chain_probe_computes_the_chains(gpu, oracle, n, kind):
     eq(res, acc)
     assert (cycles > 0).all()
     assert (prod_rounds <= 32).all() and (sum_rounds <= 32).all()
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_integer_leaves_match_directed_products(gpu, n):
+    """The fraction-sum leaves formed on the integer pipes (the exact 84-bit
+    product s * R rounded to 53 bits) are the doubles __dmul_ru / __dmul_rd give
+    for every residue tried: random ones and the edges 0, 1, 2^k, m_i - 1."""
+    rng = np.random.default_rng(helpers.SEED + 970 + n)
+    mods = np.array(helpers.moduli(n), dtype=np.int64)
+    rows = [rng.integers(0, mods) for _ in range(20000)]
+    rows += [np.zeros(n, np.int64), np.ones(n, np.int64), mods - 1, mods // 2]
+    rows += [np.minimum(np.full(n, 1 << k, np.int64), mods - 1) for k in range(31)]
+    digits = np.array(rows, dtype=np.int64).astype(np.int32)
+    r = gpu.probe_int_leaves(n, digits)
+    assert (r[:, 0] == r[:, 1]).all(), "upward leaves differ at %s" % np.flatnonzero(r[:, 0] != r[:, 1])[:5]
+    assert (r[:, 2] == r[:, 3]).all(), "downward leaves differ at %s" % np.flatnonzero(r[:, 2] != r[:, 3])[:5]
