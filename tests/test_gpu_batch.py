@@ -1,6 +1,6 @@
 """Batches (one persistent launch for many operations) against the plain entry
-points: every GEMV, DOT and SpMV (CSR, CSR-vector, ELL) output of a batch
-must equal, record for record, what mpres_gemv / mpres_dot / mpres_spmv_* give
+points: every GEMV, GEMM, DOT and SpMV (CSR, CSR-vector, ELL) output of a batch
+must equal, record for record, what mpres_gemv / mpres_gemm / mpres_dot / mpres_spmv_* give
 for the same arguments -- with and without graph replay and autotuning, for
 uneven sizes, strides, transposition, odd blockDim3 and skipped operations."""
 import numpy as np
@@ -29,7 +29,10 @@ GEMVS = [  # trans, m, n, incx, incy, b3
 DOTS = [(1, 1, 1, 256, 64), (1000, 1, 1, 256, 64), (5000, -1, 2, 7, 33), (3000, 1, 1, 64, 128), (0, 1, 1, 256, 64)]
 
 
-def _build(gpu, n, rng, small):
+GEMMS = [(1, 1, 1), (33, 7, 50), (100, 64, 129), (64, 65, 3), (130, 40, 257)]  # m, n, k
+
+
+def _build(gpu, n, rng, small, gemm=False):
     scale = 4 if small else 1
     ops = []
     for trans, m, k, incx, incy, b3 in GEMVS:
@@ -58,6 +61,13 @@ def _build(gpu, n, rng, small):
     irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m, kmax=150))
     maxnzr, eja, eas = helpers.csr_to_ell(m, irp, ja, vals)
     ops.append(dict(kind="ell", m=m, ell=gpu.DeviceEll(m, maxnzr, eja, eas), x=_vec(gpu, n, rng, m, -16, 16)))
+    if gemm:
+        for m, cols, k in GEMMS:
+            m, cols, k = max(m // scale, 1), max(cols // scale, 1), max(k // scale, 1)
+            lda, ldb, ldc = m + int(rng.integers(0, 3)), k + int(rng.integers(0, 2)), m + int(rng.integers(0, 2))
+            ops.append(dict(kind="gemm", m=m, n=cols, k=k, lda=lda, ldb=ldb, ldc=ldc,
+                            A=_vec(gpu, n, rng, lda * k), B=_vec(gpu, n, rng, ldb * cols), C=_vec(gpu, n, rng, ldc * cols),
+                            alpha=_vec(gpu, n, rng, 1, -1, 1), beta=_vec(gpu, n, rng, 1, -1, 1)))
     return ops
 
 
@@ -76,6 +86,12 @@ def _plain(gpu, n, ops):
             r = gpu.DeviceArray.from_host(n, o["r"])
             gpu.dot(n, o["n"], x, y, r, o["incx"], o["incy"], order=(512, 128, 8192, o["g3"], o["b3"]))
             out.append(r.download())
+        elif o["kind"] == "gemm":
+            A, B = gpu.DeviceArray.from_host(n, o["A"]), gpu.DeviceArray.from_host(n, o["B"])
+            al, be = gpu.DeviceArray.from_host(n, o["alpha"]), gpu.DeviceArray.from_host(n, o["beta"])
+            C = gpu.DeviceArray.from_host(n, o["C"])
+            gpu.gemm(n, o["m"], o["n"], o["k"], al, A, o["lda"], B, o["ldb"], be, C, o["ldc"])
+            out.append(C.download())
         else:
             x = gpu.DeviceBytes.from_numpy(o["x"])
             y = gpu.DeviceBytes(o["m"] * (4 * n + 40))
@@ -105,6 +121,12 @@ def _batched(gpu, n, ops, flags, runs=1):
             r = gpu.DeviceArray.from_host(n, o["r"])
             b.add_dot(o["n"], x, y, r, o["incx"], o["incy"], o["g3"], o["b3"])
             outs.append(r)
+        elif o["kind"] == "gemm":
+            A, B = gpu.DeviceArray.from_host(n, o["A"]), gpu.DeviceArray.from_host(n, o["B"])
+            al, be = gpu.DeviceArray.from_host(n, o["alpha"]), gpu.DeviceArray.from_host(n, o["beta"])
+            C = gpu.DeviceArray.from_host(n, o["C"])
+            b.add_gemm(o["m"], o["n"], o["k"], al, A, o["lda"], B, o["ldb"], be, C, o["ldc"])
+            outs.append(C)
         else:
             x = gpu.DeviceBytes.from_numpy(o["x"])
             y = gpu.DeviceBytes(o["m"] * (4 * n + 40))
@@ -125,13 +147,15 @@ def _batched(gpu, n, ops, flags, runs=1):
 
 @pytest.mark.parametrize("n", [8, 16, 32])
 @pytest.mark.parametrize("flags", [0, 1, 3])
-def test_batch_matches_plain_calls(gpu, n, flags):
+@pytest.mark.parametrize("gemm", [False, True])
+def test_batch_matches_plain_calls(gpu, n, flags, gemm):
+    """With GEMMs in the batch, the GEMM variant of the kernel runs every task."""
     rng = np.random.default_rng(helpers.SEED + 980 + n)
-    ops = _build(gpu, n, rng, small=(n == 32))
+    ops = _build(gpu, n, rng, small=(n == 32), gemm=gemm)
     want = _plain(gpu, n, ops)
     got, info = _batched(gpu, n, ops, flags)
     live = [o for o in ops if (o["kind"] == "gemv" and o["m"] > 0 and o["n"] > 0 and o["incx"] and o["incy"])
-            or (o["kind"] == "dot" and o["n"] > 0) or o["kind"] in ("spmv", "csrv", "ell")]
+            or (o["kind"] == "dot" and o["n"] > 0) or o["kind"] in ("spmv", "csrv", "ell", "gemm")]
     assert info["ops"] == len(live)  # the others are quick returns
     assert info["graph"] == (flags & 1)
     assert info["autotuned"] == (1 if flags & 2 else 0)
@@ -150,3 +174,29 @@ def test_batch_replay_reads_current_operands(gpu):
     got, _ = _batched(gpu, n, ops, gpu.BATCH_GRAPH, runs=2)
     for g, w in zip(got, second):
         eq(g, w, "second run")
+
+
+def test_batch_of_uneven_gemms_autotuned(gpu):
+    """Only GEMMs, 32 moduli, m, n, k from 3 to 150: autotuned and replayed from
+    the graph, every C equals the plain mpres_gemm's."""
+    n = 32
+    rng = np.random.default_rng(helpers.SEED + 995)
+    ops = []
+    for m, cols, k in rng.integers(3, 151, (12, 3)):
+        m, cols, k = int(m), int(cols), int(k)
+        ops.append(dict(kind="gemm", m=m, n=cols, k=k, lda=m, ldb=k, ldc=m, A=_vec(gpu, n, rng, m * k),
+                        B=_vec(gpu, n, rng, k * cols), C=_vec(gpu, n, rng, m * cols),
+                        alpha=_vec(gpu, n, rng, 1, -1, 1), beta=_vec(gpu, n, rng, 1, -1, 1)))
+    want = _plain(gpu, n, ops)
+    got, info = _batched(gpu, n, ops, gpu.BATCH_GRAPH | gpu.BATCH_AUTOTUNE)
+    assert info["threads"] in (128, 256)
+    for o, g, w in zip(ops, got, want):
+        eq(g, w, "gemm %dx%dx%d" % (o["m"], o["n"], o["k"]))
+
+
+def test_batch_gemm_rejects_transposition(gpu):
+    n = 8
+    a = gpu.DeviceArray.from_host(n, gpu.set_d(n, np.ones(4)))
+    b = gpu.Batch(n)
+    with pytest.raises(gpu.MpresError):
+        b.add_gemm(2, 2, 2, a, a, 2, a, 2, a, a, 2, transa=gpu.TRANS)
