@@ -656,6 +656,77 @@ def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
                     "alpha, beta ~ U(-1, 1)"}
 
 
+def bench_batched_gemm(torch, mp, stream, count=256):
+    """256 mp_gemm C = alpha*A*B + beta*C with m, n, k independently
+    log-uniform in [32, 512], 32 moduli, entries u*2^e (e in [-32, 32]): one
+    persistent launch (graph replay, autotuned shape, the W(A), W(B) pass
+    before it) against the 256 plain mpres_gemm calls, both timed with CUDA
+    events from the same C, outputs compared record for record."""
+    n = 32
+    sizes = log_uniform_ints(np.random.default_rng(SEED + 5), (count, 3), 32, 512)
+    pool, gen = value_pool(torch, mp, n, 1 << 22, -32, 32, SEED + 5)
+    M, Nc, K = sizes[:, 0], sizes[:, 1], sizes[:, 2]
+    a_off = np.concatenate([[0], np.cumsum(M * K)])
+    b_off = np.concatenate([[0], np.cumsum(K * Nc)])
+    c_off = np.concatenate([[0], np.cumsum(M * Nc)])
+    A, B, C = (mp.TensorArray(n, int(o[-1])) for o in (a_off, b_off, c_off))
+    for arr in (A, B, C):
+        fill_from_pool(torch, arr, pool, gen)
+    AB = mp.TensorArray(n, 2 * count)
+    AB.set_d(torch.rand(2 * count, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1)
+    ops = [(int(M[j]), int(Nc[j]), int(K[j]), AB.view(2 * j, 1), A.view(int(a_off[j]), int(M[j] * K[j])),
+            B.view(int(b_off[j]), int(K[j] * Nc[j])), AB.view(2 * j + 1, 1), C.view(int(c_off[j]), int(M[j] * Nc[j])))
+           for j in range(count)]
+    torch.cuda.synchronize()
+
+    def plain():
+        for m, c, k, al, Av, Bv, be, Cv in ops:
+            mp.gemm(n, m, c, k, al, Av, m, Bv, k, be, Cv, m, stream=stream)
+
+    batch = mp.Batch(n)
+    for m, c, k, al, Av, Bv, be, Cv in ops:
+        batch.add_gemm(m, c, k, al, Av, m, Bv, k, be, Cv, m)
+    t0 = time.perf_counter()
+    batch.commit(mp.BATCH_GRAPH | mp.BATCH_AUTOTUNE, stream=stream)
+    torch.cuda.synchronize()
+    commit_s = time.perf_counter() - t0
+    c0 = snapshot(C)
+    plain()  # warm: workspace growth and attributes
+    batch.run(stream)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    t_plain = t_batch = 0.0
+    reps = 3
+    identical = True
+    for _ in range(reps):
+        restore(C, c0)
+        torch.cuda.synchronize()
+        ev[0].record(stream)
+        plain()
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        cp = snapshot(C)
+        restore(C, c0)
+        torch.cuda.synchronize()
+        ev[2].record(stream)
+        batch.run(stream)
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        identical = identical and same(C, cp)
+        t_plain += ev[0].elapsed_time(ev[1]) / 1e3 / reps
+        t_batch += ev[2].elapsed_time(ev[3]) / 1e3 / reps
+        del cp
+    info = batch.info()
+    batch.destroy()
+    ops_total = float(np.sum(2.0 * M * Nc * K + 3.0 * M * Nc))
+    return {"workload": "256 x mp_gemm NN, m, n, k log-uniform in [32, 512], 32 moduli", "value": ops_total / t_batch,
+            "unit": "MP ops/s", "plain_value": ops_total / t_plain, "speedup_vs_plain": t_plain / t_batch,
+            "ms_batched": t_batch * 1e3, "ms_plain": t_plain * 1e3, "launches_batched": 2, "launches_plain": 3 * count,
+            "bit_identical": identical, "shape": info, "commit_s": commit_s,
+            "data": "A, B, C: random draws from 2^22 seeded u*2^e values (e in [-32, 32]) converted on the GPU; "
+                    "alpha, beta ~ U(-1, 1)"}
+
+
 def bench_serving(torch, mp, rates=(100.0, 400.0, 1600.0), duration=1.5, budget=64 << 30):
     """Poisson request streams mixing mp_dot (n log-uniform 2^10..2^22),
     mp_gemv (m, n log-uniform 32..4096) and mp_spmv_csr (rows log-uniform
@@ -1012,6 +1083,7 @@ def main():
         extra["mp_spmv"] = {k: v for k, v in spmv.items() if k != "data"}
         if not args.no_batch:
             extra["batched_gemv"] = bench_batched_gemv(torch, mp, stream, hbm)
+            extra["batched_gemm"] = bench_batched_gemm(torch, mp, stream)
             extra["serving"] = bench_serving(torch, mp)
     line = {
         "metric": METRIC, "value": g["value"], "unit": "MP ops/s", "n_gpus": world, "steps": args.steps,

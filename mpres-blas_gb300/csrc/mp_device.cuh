@@ -446,9 +446,12 @@ template <int N> __device__ __forceinline__ int pow2_row_index(int r) {
 #endif
 
 /* Refinement loop of rns_eval_compute[_fast], src/rns.cuh:843-867 / :908-932,
- * on the FP64 pipe: sumu is the current upper fraction, below RNS_EVAL_ACCURACY */
+ * on the FP64 pipe: sumu is the current upper fraction, below RNS_EVAL_ACCURACY.
+ * Inlined: it is reached from the out-of-line rounding (round_slow) and from
+ * the element-wise evaluation, and inline the residues stay in registers
+ * instead of local memory. */
 template <int N>
-__device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &upp) {
+__device__ __forceinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &upp) {
     const Tables<N> &t = T<N>();
     int K = 0;
     for (int guard = 0; dbits(sumu) < dbits(t.eval_acc) && guard < 4096; guard++) {
@@ -477,7 +480,7 @@ __device__ __noinline__ void eval_refine(int *s, double sumu, er_t &low, er_t &u
 
 /* the same loop in fixed point: fu is the current upper fraction */
 template <int N>
-__device__ __noinline__ void eval_refine(int *s, fx fu, er_t &low, er_t &upp) {
+__device__ __forceinline__ void eval_refine(int *s, fx fu, er_t &low, er_t &upp) {
     const Tables<N> &t = T<N>();
     int K = 0;
     for (int guard = 0; !fx_ge_acc<N>(fu) && guard < 4096; guard++) {
@@ -576,6 +579,24 @@ template <int N> __device__ __forceinline__ bool rank_shortcut(const int *s, uns
     return top <= (1ull << 42) - 9;
 }
 
+/* The rank of a number known to satisfy X/M < 2^-40 (from its interval
+ * evaluation): then frac(V) = X/M < 2^-40 and, as above, rank_full and
+ * rank_fast both give floor(V).  With S = sum_i s_i * ceil(2^94 / m_i),
+ * V <= S / 2^94 < V + 2^-58, so floor(S / 2^94) = floor(V) exactly (frac(V)
+ * is far from 1).  No FP64 sums and no mixed-radix digit: a rounding's ranks
+ * otherwise take the mrd branch of rank_full almost every time, because with
+ * X/M that small the directed sums straddle the integer. */
+template <int N> __device__ __forceinline__ int rank_tiny(const int *s) {
+    const Tables<N> &t = T<N>();
+    unsigned __int128 S = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) S += (unsigned __int128)(uint32_t)s[i] * (t.inv94[i] + 1);
+    return (int)(S >> 94);
+}
+/* X/M < 2^kTinyExp is what rank_tiny needs, with a 2^4 margin */
+constexpr int kTinyExp = -44;
+constexpr int kNoBound = 1 << 30;
+
 /* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */
 template <int N> __device__ __forceinline__ int rank_full(const int *x, const int *s) {
     unsigned int fast;
@@ -624,29 +645,35 @@ __device__ __forceinline__ void scaling_step(int *y, int k, int j, const int *x,
     }
 }
 
-/* cuda::rns_scale2pow, src/rns.cuh:1132-1158; in place */
-template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int D) {
+/* cuda::rns_scale2pow, src/rns.cuh:1132-1158; in place.  ebound: X/M < 2^ebound
+ * is known (from the number's interval evaluation; kNoBound when nothing is);
+ * every step divides X by 2^j, so the bound drops by j, and while it is at most
+ * kTinyExp the ranks come from rank_tiny -- the values the reference's ranks
+ * take there. */
+template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int D, int ebound = kNoBound) {
     const Tables<N> &t = T<N>();
     int c[N];
     int steps = (int)(D / kScaleBits);
     if (steps > 0) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = rank_full<N>(x, c);
+        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : rank_full<N>(x, c);
         scaling_step<N>(x, k, kScaleBits, x, c);
         steps -= 1;
+        ebound -= kScaleBits;
     }
     for (; steps > 0; steps--) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = rank_fast<N>(c);
+        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : rank_fast<N>(c);
         scaling_step<N>(x, k, kScaleBits, x, c);
+        ebound -= kScaleBits;
     }
     unsigned int d = D % kScaleBits;
     if (d > 0) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = (d < D) ? rank_full<N>(x, c) : rank_fast<N>(c);
+        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : ((d < D) ? rank_full<N>(x, c) : rank_fast<N>(c));
         scaling_step<N>(x, k, (int)d, x, c);
     }
 }
@@ -656,7 +683,10 @@ template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int 
  * mp_matrix_round_kernel (src/mpmatrix.cuh:410-428). */
 template <int N> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
     r.exp += bits;
-    scale2pow<N>(r.d, (unsigned int)bits);
+    /* the upper bound of the interval evaluation: X/M <= frac * 2^exp with frac
+     * in [1, 2) (er_adjust), so X/M < 2^(exp + 1) */
+    const long long ub = r.ev[1].exp + 1;
+    scale2pow<N>(r.d, (unsigned int)bits, (dpos(r.ev[1].frac) && ub <= kTinyExp) ? (int)ub : kNoBound);
     eval_fast<N>(r.ev[0], r.ev[1], r.d);
 }
 /* The out-of-line calls of the rare paths take their operands through a copy:
