@@ -681,23 +681,30 @@ template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int 
 /* Rounding after an operation: src/arith/arith_utils.cuh:172-190 (mp_round with
  * mp_get_rnd_bits), also mp_vector_round_kernel (src/mpvector.cuh:669-688) and
  * mp_matrix_round_kernel (src/mpmatrix.cuh:410-428). */
-template <int N> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
+/* BOUNDED: the number's interval evaluation bounds X/M from above, as it does
+ * after mp_add, mp_mul and mp_mul_d when their operands' evaluations bound
+ * theirs (the bounds are computed with directed rounding); the scaling's ranks
+ * may then use the bound.  Not after the GEMM's split addition, which takes the
+ * sign from the interval alone and can store a negative sum as M - |sum| under
+ * a small bound. */
+template <int N, bool BOUNDED> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
     r.exp += bits;
     /* the upper bound of the interval evaluation: X/M <= frac * 2^exp with frac
      * in [1, 2) (er_adjust), so X/M < 2^(exp + 1) */
     const long long ub = r.ev[1].exp + 1;
-    scale2pow<N>(r.d, (unsigned int)bits, (dpos(r.ev[1].frac) && ub <= kTinyExp) ? (int)ub : kNoBound);
+    scale2pow<N>(r.d, (unsigned int)bits,
+                 (BOUNDED && dpos(r.ev[1].frac) && ub <= kTinyExp) ? (int)ub : kNoBound);
     eval_fast<N>(r.ev[0], r.ev[1], r.d);
 }
 /* The out-of-line calls of the rare paths take their operands through a copy:
  * a variable whose address reaches a call lives in local memory, so passing
  * the caller's own number would keep every number of the hot loop there. */
-template <int N> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
+template <int N, bool BOUNDED = true> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
     if (dnz(r.ev[1].frac) && r.ev[1].exp >= T<N>().mp_h) {
         int bits = (int)(r.ev[1].exp - T<N>().mp_h + 1);
         if (bits > 0) {
             mp_t<N> tmp = r;
-            round_slow<N>(tmp, bits);
+            round_slow<N, BOUNDED>(tmp, bits);
             r = tmp;
         }
     }
