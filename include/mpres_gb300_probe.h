@@ -78,6 +78,15 @@ int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int cou
 int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long count, void *result, int *out,
                              void *stream);
 
+/* The phases of the interval evaluation rns_eval_compute_fast, one warp alone:
+ * digits = int[32*count*nmod] (lane l takes numbers l*count ..
+ * l*count+count-1); cycles = long long[40*count] receives lane 0's SM cycles
+ * per number: {initial products and upward sum, refinement steps taken, final
+ * downward sum, clock-fence overhead, then for each of up to 12 refinement
+ * steps: ceil(log2) and row index, row load and modular products, upward
+ * sum}; out = int[32] checksum.  Device memory. */
+int mpres_probe_eval_phases(int nmod, const int *digits, int count, long long *cycles, int *out, void *stream);
+
 /* Element-wise device arithmetic over AoS mp_float_t vectors (device memory), one
  * element per thread: the device functions the BLAS kernels are built from,
  * exposed so that each can be checked against the reference on its own.

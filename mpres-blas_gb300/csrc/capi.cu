@@ -802,6 +802,14 @@ int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long c
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_fraction_sum");
 }
 
+int mpres_probe_eval_phases(int nmod, const int *digits, int count, long long *cycles, int *out, void *stream) {
+    if (int st = require(nmod)) return st;
+    if (count <= 0 || !digits || !cycles || !out)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_eval_phases: bad arguments");
+    cudaError_t e = launch_eval_phase_probe(nmod, digits, count, cycles, out, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_eval_phases");
+}
+
 int mpres_rns_scale2pow(int nmod, const int *digits, const unsigned *D, int *out, size_t count, void *stream) {
     if (int st = require(nmod)) return st;
     if (count == 0) return ok();

@@ -219,10 +219,95 @@ template <int N> __global__ void int_leaf_check(const int *digits, long long cou
     }
 }
 
+/* the SM clock once v is computed: a shared-memory store of v (which waits for
+ * it) and a block fence (which waits for the store) come first */
+__device__ __forceinline__ long long clock_after(uint64_t v, volatile uint64_t *sink) {
+    *sink = v;
+    __threadfence_block();
+    return clock64();
+}
+
+/* The phases of rns_eval_compute_fast (mp_device.cuh's eval_fast, FP64 form),
+ * one warp alone, for `count` numbers per lane (lane l: digits of numbers
+ * l*count .. l*count+count-1).  Lane 0 writes per number 4 + 3*12 counters:
+ * [0] the part_inv products and the upward sum, [1] the number of refinement
+ * steps, [2] the final downward sum, [3] the fence overhead of one clock_after;
+ * then per refinement step j < 12: [4+3j] ceil(log2) and the row index, [5+3j]
+ * the row load and the N modular products, [6+3j] the upward sum. */
+template <int N> __global__ void eval_phase_probe(const int *digits, int count, long long *cycles, int *out) {
+    const Tables<N> &t = T<N>();
+    __shared__ uint64_t sink[32];
+    volatile uint64_t *mine = sink + threadIdx.x;
+    const int lane = threadIdx.x;
+    int acc = 0;
+    for (int j = 0; j < count; j++) {
+        long long c[4 + 36] = {};
+        const long long e = (long long)lane * count + j;
+        int s[N];
+#pragma unroll
+        for (int i = 0; i < N; i++) s[i] = __ldg(digits + e * N + i);
+        long long t0 = clock_after((uint64_t)s[N - 1], mine);
+        const long long t00 = clock_after((uint64_t)s[0], mine);
+        c[3] = t00 - t0;
+        t0 = t00;
+#pragma unroll
+        for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], t.part_inv[i], i);
+        double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
+        sumu = d_frac<true>(sumu);
+        long long t1 = clock_after(dbits(sumu), mine);
+        c[0] = t1 - t0;
+        int it = 0;
+        for (int guard = 0; dbits(sumu) < dbits(t.eval_acc) && guard < 4096; guard++) {
+            int k;
+            if (!dnz(sumu)) {
+                k = t.log2m;
+            } else {
+                const int cl = ceil_log2_d<N>(sumu);
+                k = -(cl + 1) > t.ref_factor ? -(cl + 1) : t.ref_factor;
+                k = pow2_row_index<N>(k < 0 ? 0 : k);
+            }
+            const long long ta = clock_after((uint64_t)k, mine);
+            const int *row = t.pow2 + (size_t)k * N;
+#pragma unroll
+            for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
+            const long long tb = clock_after((uint64_t)s[N - 1] + (uint64_t)s[0], mine);
+            sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
+            sumu = d_frac<true>(sumu);
+            const long long tc = clock_after(dbits(sumu), mine);
+            if (it < 12) {
+                c[4 + 3 * it] = ta - t1;
+                c[5 + 3 * it] = tb - ta;
+                c[6 + 3 * it] = tc - tb;
+            }
+            t1 = tc;
+            it++;
+        }
+        c[1] = it;
+        const double suml =
+            d_frac<false>(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
+        const long long t2 = clock_after(dbits(suml), mine);
+        c[2] = t2 - t1;
+        acc += (int)(dbits(suml) >> 33);
+        if (lane == 0)
+            for (int q = 0; q < 40; q++) cycles[(long long)j * 40 + q] = c[q];
+    }
+    out[lane] = acc;
+}
+
 } // namespace chainprobe
 } // namespace mpres
 
 /* the host launchers of this translation unit's instantiations */
+#define MPRES_EVAL_PHASE_LAUNCHER(NAME)                                                                            \
+    cudaError_t NAME(int nmod, const int *digits, int count, long long *cycles, int *out, cudaStream_t s) {     \
+        switch (nmod) {                                                                                            \
+        case 8: chainprobe::eval_phase_probe<8><<<1, 32, 0, s>>>(digits, count, cycles, out); break;               \
+        case 16: chainprobe::eval_phase_probe<16><<<1, 32, 0, s>>>(digits, count, cycles, out); break;             \
+        case 32: chainprobe::eval_phase_probe<32><<<1, 32, 0, s>>>(digits, count, cycles, out); break;             \
+        default: return cudaErrorInvalidValue;                                                                     \
+        }                                                                                                          \
+        return cudaGetLastError();                                                                                 \
+    }
 #define MPRES_PSUM_PROBE_LAUNCHER(NAME)                                                                        \
     cudaError_t NAME(int nmod, int which, const int *digits, long long count, void *cycles_or_out, int *out,  \
                      cudaStream_t s) {                                                                          \

@@ -211,5 +211,6 @@ cudaError_t launch_check(int which, int nmod, const void *a, const void *b, void
 MPRES_CHAIN_PROBE_LAUNCHER(launch_chain_probe_fp64)
 MPRES_ROUND_PROBE_LAUNCHER(launch_round_probe)
 MPRES_PSUM_PROBE_LAUNCHER(launch_psum_probe)
+MPRES_EVAL_PHASE_LAUNCHER(launch_eval_phase_probe)
 
 } // namespace mpres

@@ -111,6 +111,7 @@ _SIGS = {
     "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_chain": (I, [I, I, P, P, I, P, P, P, P]),
     "mpres_probe_rounding": (I, [I, P, P, I, P, P, I, P]),
+    "mpres_probe_eval_phases": (I, [I, P, I, P, P, P]),
     "mpres_probe_fraction_sum": (I, [I, I, P, ctypes.c_longlong, P, P, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
     "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
@@ -757,6 +758,17 @@ def probe_rounding(nmod, digits, D, count, bound_offset=1 << 30):
           "mpres_probe_rounding")
     torch.cuda.synchronize()
     return cyc.to_numpy(np.int64, 5 * count).reshape(count, 5)
+
+
+def probe_eval_phases(nmod, digits, count):
+    """Cycles of the interval evaluation's phases (mpres_probe_eval_phases) for
+    32*count numbers digits int32[32*count, nmod]; returns int64[count, 40]."""
+    import torch
+    dd = DeviceBytes.from_numpy(np.ascontiguousarray(digits, dtype=np.int32))
+    cyc, out = DeviceBytes(8 * 40 * count), DeviceBytes(4 * 32)
+    check(lib().mpres_probe_eval_phases(nmod, dd.ptr, count, cyc.ptr, out.ptr, None), "mpres_probe_eval_phases")
+    torch.cuda.synchronize()
+    return cyc.to_numpy(np.int64, 40 * count).reshape(count, 40)
 
 
 def probe_fraction_sum_cycles(nmod, digits, reps=64):
