@@ -62,11 +62,9 @@ int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len,
  * bits to round away; cycles = long long[count*5] receives lane 0's SM cycles
  * per number of {rns_scale2pow, rns_eval_compute_fast, one upward fraction
  * sum, the modular products of one refinement step, rank_full}; out = int[32]
- * (a checksum).  bound_offset: the scaling is told X/M < 2^(D + bound_offset)
- * as a rounding knows it from the interval evaluation (1 << 30: nothing is
- * known).  Device memory. */
+ * (a checksum).  Device memory. */
 int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
-                         int bound_offset, void *stream);
+                         void *stream);
 
 /* The upward fraction sum of the interval evaluation three ways, exact and
  * bit-identical: which 0 times `count` dependent sums on one warp for each form

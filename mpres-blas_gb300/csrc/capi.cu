@@ -784,12 +784,11 @@ int mpres_probe_chain(int nmod, int kind, const void *x, const void *y, int len,
 }
 
 int mpres_probe_rounding(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
-                         int bound_offset, void *stream) {
+                         void *stream) {
     if (int st = require(nmod)) return st;
     if (count <= 0 || !digits || !D || !cycles || !out)
         return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_rounding: bad arguments");
-    cudaError_t e = launch_round_probe(nmod, digits, D, count, cycles, out, bound_offset,
-                                       static_cast<cudaStream_t>(stream));
+    cudaError_t e = launch_round_probe(nmod, digits, D, count, cycles, out, static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_rounding");
 }
 

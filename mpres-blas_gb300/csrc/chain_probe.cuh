@@ -88,8 +88,7 @@ __global__ void chain_probe(int kind, const void *x, const void *y, int len, lon
  *   [4] rank_full of the input (the first scaling step's rank).
  * Results are written to `out` so nothing is optimised away. */
 template <int N>
-__global__ void round_parts_probe(const int *digits, const unsigned *D, int count, long long *cycles, int *out,
-                                  int bound_offset) {
+__global__ void round_parts_probe(const int *digits, const unsigned *D, int count, long long *cycles, int *out) {
     const Tables<N> &t = T<N>();
     const int lane = threadIdx.x;
     int acc = 0;
@@ -107,8 +106,7 @@ __global__ void round_parts_probe(const int *digits, const unsigned *D, int coun
         acc += rk;
         __syncwarp();
         long long t1 = clock64();
-        /* bound_offset: X/M < 2^(D + bound_offset) is known (kNoBound: nothing is) */
-        scale2pow<N>(d, bits, bound_offset == kNoBound ? kNoBound : (int)bits + bound_offset);
+        scale2pow<N>(d, bits);
         acc += d[0];
         __syncwarp();
         long long t2 = clock64();
@@ -329,11 +327,11 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
     }
 #define MPRES_ROUND_PROBE_LAUNCHER(NAME)                                                                      \
     cudaError_t NAME(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,  \
-                     int bound_offset, cudaStream_t s) {                                                      \
+                     cudaStream_t s) {                                                                        \
         switch (nmod) {                                                                                       \
-        case 8: chainprobe::round_parts_probe<8><<<1, 32, 0, s>>>(digits, D, count, cycles, out, bound_offset); break;   \
-        case 16: chainprobe::round_parts_probe<16><<<1, 32, 0, s>>>(digits, D, count, cycles, out, bound_offset); break; \
-        case 32: chainprobe::round_parts_probe<32><<<1, 32, 0, s>>>(digits, D, count, cycles, out, bound_offset); break; \
+        case 8: chainprobe::round_parts_probe<8><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;      \
+        case 16: chainprobe::round_parts_probe<16><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;    \
+        case 32: chainprobe::round_parts_probe<32><<<1, 32, 0, s>>>(digits, D, count, cycles, out); break;    \
         default: return cudaErrorInvalidValue;                                                                \
         }                                                                                                     \
         return cudaGetLastError();                                                                            \

@@ -40,8 +40,6 @@
  * interval evaluation (out-of-line steps, epilogue, step-by-step chain) runs in
  * fixed point on the integer pipes (mp_device.cuh) */
 #define MPRES_EVAL_FIXED_POINT 1
-#include <cstdlib>
-
 #include "kernels.h"
 #include "mp_device.cuh"
 #include "gemm_chain.cuh"
@@ -103,15 +101,6 @@ __global__ void __launch_bounds__(256) gemm_prescale(const int *digits, const in
     prescale_element<N, A_LAYOUT>(digits, sign, exp, ld, rows, e, out);
 }
 
-template <int N, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY, 3) gemm_nn_lazy(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
-                                                       int ldb, SoA beta, int *cd, int *cs, int *ce, er_t *cv,
-                                                       const int *clen, int ldc, const int4 *WA, const int4 *WB) {
-    const int row = blockIdx.x * BX + threadIdx.x;
-    const int col = blockIdx.y * BY + threadIdx.y;
-    if (row >= m || col >= n) return;
-    gemm_lazy_output<N>(m, k, alpha, A, lda, B, ldb, beta, cd, cs, ce, cv, clen, ldc, WA, WB, row, col);
-}
 
 /* ------------- the scalar half of a step with 32-bit exponents --------------
  *
@@ -273,7 +262,8 @@ __device__ __forceinline__ void widen32(const Scal32 &x, Scal &y) {
 
 /* ------------------- the k chain with shared-memory k tiles ------------------
  *
- * The same lazy-residue chain as gemm_nn_lazy, with its operands staged: for
+ * The lazy-residue chain of gemm_lazy_output (gemm_chain.cuh, which the batch
+ * kernel runs per thread), with its operands staged: for
  * every KT consecutive k steps the block copies, with cp.async into a second
  * buffer while it works on the first,
  *   W(A) of its 32 rows (KT x N/4 x 32 int4), W(B) of its 4 columns
@@ -352,8 +342,8 @@ __device__ __forceinline__ void stage_tile(GemmTile<N, BX, BY> &tl, int k0, int 
     }
 }
 
-template <int N, int BX, int BY, int MINB>
-__global__ void __launch_bounds__(BX *BY, MINB) gemm_nn_tiled(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
+template <int N, int BX, int BY>
+__global__ void __launch_bounds__(BX *BY, 4) gemm_nn_tiled(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
                                                           int ldb, SoA beta, int *cd, int *cs, int *ce, er_t *cv,
                                                           const int *clen, int ldc, const int4 *WA, const int4 *WB) {
     constexpr int Q = N / 4;
@@ -398,7 +388,7 @@ __global__ void __launch_bounds__(BX *BY, MINB) gemm_nn_tiled(int m, int n, int 
             const uint32_t wa_s = (uint32_t)__cvta_generic_to_shared(&tl.wa[0][0][tx]);
             const uint32_t wb_s = (uint32_t)__cvta_generic_to_shared(&tl.wb[0][ty][0]);
             /* the steps that stay lazy run in the inner loop, which leaves at the
-             * first that does not; that step runs out of line (as in gemm_nn_lazy).
+             * first that does not; that step runs out of line (as in gemm_lazy_output).
              * The inner loop carries the sum's scalars in the 32-bit form. */
             int kk = 0;
             for (;;) {
@@ -516,33 +506,19 @@ cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &
         const long long na = (long long)m * k, nb = (long long)k * n;
         gemm_prescale<N, true><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A.digits, A.sign, A.exp, lda, m, k, wa);
         gemm_prescale<N, false><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, wb);
-        const char *v1 = std::getenv("MPRES_GEMM_V1");
-        if (v1 && v1[0] == '1') {
-            gemm_nn_lazy<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta),
-                                                           C.digits, C.sign, C.exp, cv, C.len, ldc, wa, wb);
-        } else {
-            constexpr size_t smem = 2 * sizeof(GemmTile<N, BX, BY>);
-            const char *mb = std::getenv("MPRES_GEMM_MINB");
-            const bool three = mb && mb[0] == '3';
-            static PerDevice<cudaError_t> attrs(cuda_ok);
-            cudaError_t e = attrs.get(current_device(), cudaErrorInvalidDevice, [] {
-                cudaError_t r = cudaFuncSetAttribute(gemm_nn_tiled<N, BX, BY, 4>,
-                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                if (r != cudaSuccess) return r;
-                return cudaFuncSetAttribute(gemm_nn_tiled<N, BX, BY, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)smem);
-            });
-            if (e != cudaSuccess) return e;
-            const unsigned blocks = grid.x * grid.y;
-            if (three)
-                gemm_nn_tiled<N, BX, BY, 3><<<blocks, block, smem, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb,
-                                                                        soa(beta), C.digits, C.sign, C.exp, cv, C.len,
-                                                                        ldc, wa, wb);
-            else
-                gemm_nn_tiled<N, BX, BY, 4><<<blocks, block, smem, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb,
-                                                                        soa(beta), C.digits, C.sign, C.exp, cv, C.len,
-                                                                        ldc, wa, wb);
-        }
+        /* one-dimensional grid in groups of row blocks; the block index
+         * arithmetic stays within int */
+        if ((long long)grid.x * grid.y > (1ll << 28)) return cudaErrorInvalidConfiguration;
+        constexpr size_t smem = 2 * sizeof(GemmTile<N, BX, BY>);
+        static PerDevice<cudaError_t> attrs(cuda_ok);
+        cudaError_t e = attrs.get(current_device(), cudaErrorInvalidDevice, [] {
+            return cudaFuncSetAttribute(gemm_nn_tiled<N, BX, BY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem);
+        });
+        if (e != cudaSuccess) return e;
+        gemm_nn_tiled<N, BX, BY><<<grid.x * grid.y, block, smem, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb,
+                                                                     soa(beta), C.digits, C.sign, C.exp, cv, C.len,
+                                                                     ldc, wa, wb);
     } else {
         gemm_nn<N, BX, BY><<<grid, block, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B), ldb, soa(beta), C.digits,
                                                   C.sign, C.exp, cv, C.len, ldc);

@@ -78,8 +78,7 @@ template <int N> __device__ __forceinline__ void split_add(mp_t<N> &res, const m
         if (minus) residue = (int)(((long long)lm - (long long)residue) % (long long)lm);
         res.d[i] = residue < 0 ? residue + lm : residue;
     }
-    /* the sign from the interval alone: the interval need not bound X/M here */
-    round_if_needed<N, false>(res);
+    round_if_needed<N>(res);
 }
 
 /* 2^e mod m for any integer e (2^-1 = (m+1)/2 for the odd m), square and multiply */

@@ -81,7 +81,7 @@ cudaError_t launch_elementwise(int nmod, int op, const void *x, const void *y, v
 cudaError_t launch_chain_probe_fp64(int nmod, int kind, const void *x, const void *y, int len, long long *cycles,
                                     unsigned *rounds, void *res, cudaStream_t s);
 cudaError_t launch_round_probe(int nmod, const int *digits, const unsigned *D, int count, long long *cycles, int *out,
-                               int bound_offset, cudaStream_t s);
+                               cudaStream_t s);
 cudaError_t launch_psum_probe(int nmod, int which, const int *digits, long long count, void *cycles_or_out, int *out,
                               cudaStream_t s);
 cudaError_t launch_eval_phase_probe(int nmod, const int *digits, int count, long long *cycles, int *out,

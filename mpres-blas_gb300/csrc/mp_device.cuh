@@ -383,40 +383,70 @@ namespace dev {
 
 /* --------------------------- RNS algorithms ------------------------------ */
 
-/* Most significant mixed-radix digit, src/rns.cuh:587-603 (cuda::mrd).  Rare
- * path (ambiguous interval evaluations): kept out of line. */
-template <int N> __device__ __noinline__ int mrd(const int *x) {
+/* One step of the mixed-radix conversion (cuda::mrc / cuda::mrd,
+ * src/rns.cuh:570-603): digit i less the finished digit j (mod_psub when it is
+ * the smaller), times m_j^-1 mod m_i. */
+template <int N> __device__ __forceinline__ int mrc_step(int v, int pivot, int j, int i) {
     const Tables<N> &t = T<N>();
-    int mixed[N];
-    for (int i = 0; i < N; i++) {
-        int v = x[i];
-        const uint32_t m = (uint32_t)t.moduli[i];
-        for (int j = 0; j < i; j++) {
-            if (v < mixed[j]) v = (int)reduce2((uint32_t)v - (uint32_t)mixed[j] + m, m);
-            else v = v - mixed[j];
-            v = (int)mulmod((uint32_t)v, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
-        }
-        mixed[i] = v;
-    }
-    return mixed[N - 1];
+    const uint32_t m = (uint32_t)t.moduli[i];
+    const uint32_t d = v < pivot ? reduce2((uint32_t)v - (uint32_t)pivot + m, m) : (uint32_t)(v - pivot);
+    return (int)mulmod(d, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
 }
 
-/* mrc_compare_rns, src/rns.cuh:570-630 (rare path) */
-template <int N> __device__ __noinline__ int mrc_compare(const int *x, const int *y) {
-    const Tables<N> &t = T<N>();
-    int mx[N], my[N];
-    for (int i = 0; i < N; i++) {
-        const uint32_t m = (uint32_t)t.moduli[i];
-        int vx = x[i], vy = y[i];
-        for (int j = 0; j < i; j++) {
-            vx = (vx < mx[j]) ? (int)reduce2((uint32_t)vx - (uint32_t)mx[j] + m, m) : vx - mx[j];
-            vx = (int)mulmod((uint32_t)vx, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
-            vy = (vy < my[j]) ? (int)reduce2((uint32_t)vy - (uint32_t)my[j] + m, m) : vy - my[j];
-            vy = (int)mulmod((uint32_t)vy, (uint32_t)t.mrc_inv[j][i], m, t.mu[i]);
+/* The mixed-radix digits of x, in place.  The reference forms digit i by the
+ * steps j = 0 .. i-1 in that order, one digit after another: a chain of
+ * N(N-1)/2 dependent modular products (measured on one warp: 3.4k cycles for
+ * 8 moduli, 15k for 16, 62k for 32).  Here every finished digit j updates all
+ * later digits at once: each digit still takes the steps j = 0 .. i-1 in order,
+ * so the values are the same, but the chain is N - 1 rounds of independent
+ * products.  Up to 16 moduli every index is a constant; for 32 the rounds are
+ * a loop and the next round's finished digit is carried in a scalar, so no
+ * digit is addressed by a runtime index (which would move them to local
+ * memory). */
+template <int N> __device__ __forceinline__ void mrc_digits(int (&v)[N]) {
+    if constexpr (N <= 16) {
+#pragma unroll
+        for (int j = 0; j < N - 1; j++) {
+#pragma unroll
+            for (int i = j + 1; i < N; i++) v[i] = mrc_step<N>(v[i], v[j], j, i);
         }
-        mx[i] = vx;
-        my[i] = vy;
+    } else {
+        int pivot = v[0];
+#pragma unroll 1
+        for (int j = 0; j < N - 1; j++) {
+            int next = 0;
+#pragma unroll
+            for (int i = 1; i < N; i++) {
+                if (i > j) {
+                    v[i] = mrc_step<N>(v[i], pivot, j, i);
+                    if (i == j + 1) next = v[i];
+                }
+            }
+            pivot = next;
+        }
     }
+}
+
+/* Most significant mixed-radix digit, src/rns.cuh:587-603 (cuda::mrd) */
+template <int N> __device__ __forceinline__ int mrd(const int *x) {
+    int v[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) v[i] = x[i];
+    mrc_digits<N>(v);
+    return v[N - 1];
+}
+
+/* mrc_compare_rns, src/rns.cuh:570-630 (rare path: ambiguous signs) */
+template <int N> __device__ __noinline__ int mrc_compare(const int *x, const int *y) {
+    int mx[N], my[N];
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+        mx[i] = x[i];
+        my[i] = y[i];
+    }
+    mrc_digits<N>(mx);
+    mrc_digits<N>(my);
+#pragma unroll
     for (int i = N - 1; i >= 0; i--) {
         if (mx[i] > my[i]) return 1;
         if (my[i] > mx[i]) return -1;
@@ -579,43 +609,43 @@ template <int N> __device__ __forceinline__ bool rank_shortcut(const int *s, uns
     return top <= (1ull << 42) - 9;
 }
 
-/* The rank of a number known to satisfy X/M < 2^-40 (from its interval
- * evaluation): then frac(V) = X/M < 2^-40 and, as above, rank_full and
- * rank_fast both give floor(V).  With S = sum_i s_i * ceil(2^94 / m_i),
- * V <= S / 2^94 < V + 2^-58, so floor(S / 2^94) = floor(V) exactly (frac(V)
- * is far from 1).  No FP64 sums and no mixed-radix digit: a rounding's ranks
- * otherwise take the mrd branch of rank_full almost every time, because with
- * X/M that small the directed sums straddle the integer. */
-template <int N> __device__ __forceinline__ int rank_tiny(const int *s) {
+/* floor(S / 2^94) for S = sum_i s_i * ceil(2^94 / m_i): V <= S / 2^94 < V + 2^-58 */
+template <int N> __device__ __forceinline__ unsigned int rank_from_above(const int *s) {
     const Tables<N> &t = T<N>();
     unsigned __int128 S = 0;
 #pragma unroll
     for (int i = 0; i < N; i++) S += (unsigned __int128)(uint32_t)s[i] * (t.inv94[i] + 1);
-    return (int)(S >> 94);
+    return (unsigned int)(S >> 94);
 }
-/* X/M < 2^kTinyExp is what rank_tiny needs, with a 2^4 margin */
-constexpr int kTinyExp = -44;
-constexpr int kNoBound = 1 << 30;
 
-/* cuda::rns_rank_compute, src/rns.cuh:1061-1079 */
+/* cuda::rns_rank_compute, src/rns.cuh:1061-1079.  When rank_shortcut cannot
+ * decide, frac(V) = X/M is within 2^-39 of an integer: in a rounding it is
+ * almost always tiny, and the directed sums straddle the integer.  The
+ * reference then takes whu when the top mixed-radix digit mrd(x) is 0 and whl
+ * otherwise.  mrd(x) = 0 means X < M / m_(N-1), so X/M < 2^-30: whu is floor(V)
+ * and floor(V) = floor(S / 2^94) with the ceiling inverses.  Otherwise
+ * (frac(V) just below 1) both branches of the reference give whl, from the
+ * downward sum. */
 template <int N> __device__ __forceinline__ int rank_full(const int *x, const int *s) {
     unsigned int fast;
     if (rank_shortcut<N>(s, fast)) return (int)fast;
+    if (mrd<N>(x) == 0) return (int)rank_from_above<N>(s);
 #if MPRES_EVAL_FIXED_POINT
-    const unsigned int whl = fx_whole(fx_fraction_sum<N, false>(s));
-    const unsigned int whu = fx_whole(fx_fraction_sum<N, true>(s));
+    return (int)fx_whole(fx_fraction_sum<N, false>(s));
 #else
     const Tables<N> &t = T<N>();
-    const unsigned int whl = d_trunc_u32(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
-    const unsigned int whu = d_trunc_u32(psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); }));
+    return (int)d_trunc_u32(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
 #endif
-    if (whl == whu) return (int)whl;
-    return (mrd<N>(x) == 0) ? (int)whu : (int)whl;
 }
-/* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096 */
-template <int N> __device__ __forceinline__ int rank_fast(const int *s) {
+/* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096: whu.  With mrd(x) = 0,
+ * X/M < 2^-30 and whu = floor(V) as above; up to 16 moduli the mixed-radix
+ * digit is cheaper than the FP64 sum, for 32 the sum is taken directly. */
+template <int N> __device__ __forceinline__ int rank_fast(const int *x, const int *s) {
     unsigned int fast;
     if (rank_shortcut<N>(s, fast)) return (int)fast;
+    if constexpr (N <= 16) {
+        if (mrd<N>(x) == 0) return (int)rank_from_above<N>(s);
+    }
 #if MPRES_EVAL_FIXED_POINT
     return (int)fx_whole(fx_fraction_sum<N, true>(s));
 #else
@@ -645,35 +675,29 @@ __device__ __forceinline__ void scaling_step(int *y, int k, int j, const int *x,
     }
 }
 
-/* cuda::rns_scale2pow, src/rns.cuh:1132-1158; in place.  ebound: X/M < 2^ebound
- * is known (from the number's interval evaluation; kNoBound when nothing is);
- * every step divides X by 2^j, so the bound drops by j, and while it is at most
- * kTinyExp the ranks come from rank_tiny -- the values the reference's ranks
- * take there. */
-template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int D, int ebound = kNoBound) {
+/* cuda::rns_scale2pow, src/rns.cuh:1132-1158; in place */
+template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int D) {
     const Tables<N> &t = T<N>();
     int c[N];
     int steps = (int)(D / kScaleBits);
     if (steps > 0) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : rank_full<N>(x, c);
+        int k = rank_full<N>(x, c);
         scaling_step<N>(x, k, kScaleBits, x, c);
         steps -= 1;
-        ebound -= kScaleBits;
     }
     for (; steps > 0; steps--) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : rank_fast<N>(c);
+        int k = rank_fast<N>(x, c);
         scaling_step<N>(x, k, kScaleBits, x, c);
-        ebound -= kScaleBits;
     }
     unsigned int d = D % kScaleBits;
     if (d > 0) {
 #pragma unroll
         for (int i = 0; i < N; i++) c[i] = mulmod_i<N>(x[i], t.part_inv[i], i);
-        int k = ebound <= kTinyExp ? rank_tiny<N>(c) : ((d < D) ? rank_full<N>(x, c) : rank_fast<N>(c));
+        int k = (d < D) ? rank_full<N>(x, c) : rank_fast<N>(x, c);
         scaling_step<N>(x, k, (int)d, x, c);
     }
 }
@@ -681,30 +705,20 @@ template <int N> __device__ __forceinline__ void scale2pow(int *x, unsigned int 
 /* Rounding after an operation: src/arith/arith_utils.cuh:172-190 (mp_round with
  * mp_get_rnd_bits), also mp_vector_round_kernel (src/mpvector.cuh:669-688) and
  * mp_matrix_round_kernel (src/mpmatrix.cuh:410-428). */
-/* BOUNDED: the number's interval evaluation bounds X/M from above, as it does
- * after mp_add, mp_mul and mp_mul_d when their operands' evaluations bound
- * theirs (the bounds are computed with directed rounding); the scaling's ranks
- * may then use the bound.  Not after the GEMM's split addition, which takes the
- * sign from the interval alone and can store a negative sum as M - |sum| under
- * a small bound. */
-template <int N, bool BOUNDED> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
+template <int N> __device__ __noinline__ void round_slow(mp_t<N> &r, int bits) {
     r.exp += bits;
-    /* the upper bound of the interval evaluation: X/M <= frac * 2^exp with frac
-     * in [1, 2) (er_adjust), so X/M < 2^(exp + 1) */
-    const long long ub = r.ev[1].exp + 1;
-    scale2pow<N>(r.d, (unsigned int)bits,
-                 (BOUNDED && dpos(r.ev[1].frac) && ub <= kTinyExp) ? (int)ub : kNoBound);
+    scale2pow<N>(r.d, (unsigned int)bits);
     eval_fast<N>(r.ev[0], r.ev[1], r.d);
 }
 /* The out-of-line calls of the rare paths take their operands through a copy:
  * a variable whose address reaches a call lives in local memory, so passing
  * the caller's own number would keep every number of the hot loop there. */
-template <int N, bool BOUNDED = true> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
+template <int N> __device__ __forceinline__ void round_if_needed(mp_t<N> &r) {
     if (dnz(r.ev[1].frac) && r.ev[1].exp >= T<N>().mp_h) {
         int bits = (int)(r.ev[1].exp - T<N>().mp_h + 1);
         if (bits > 0) {
             mp_t<N> tmp = r;
-            round_slow<N, BOUNDED>(tmp, bits);
+            round_slow<N>(tmp, bits);
             r = tmp;
         }
     }

@@ -110,7 +110,7 @@ _SIGS = {
     "mpres_probe_ceil_log2": (I, [P, P, SZ, P]),
     "mpres_probe_check": (I, [I, I, P, P, P, SZ, P]),
     "mpres_probe_chain": (I, [I, I, P, P, I, P, P, P, P]),
-    "mpres_probe_rounding": (I, [I, P, P, I, P, P, I, P]),
+    "mpres_probe_rounding": (I, [I, P, P, I, P, P, P]),
     "mpres_probe_eval_phases": (I, [I, P, I, P, P, P]),
     "mpres_probe_fraction_sum": (I, [I, I, P, ctypes.c_longlong, P, P, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
@@ -746,7 +746,7 @@ def probe_chain(nmod, kind, x, y, length):
             res.to_numpy(x.dtype, 32))
 
 
-def probe_rounding(nmod, digits, D, count, bound_offset=1 << 30):
+def probe_rounding(nmod, digits, D, count):
     """Cycles of a rounding's parts (mpres_probe_rounding) for 32*count numbers:
     digits int32[32*count, nmod], D uint32[32*count]; returns int64[count, 5]."""
     import torch
@@ -754,8 +754,7 @@ def probe_rounding(nmod, digits, D, count, bound_offset=1 << 30):
     D = np.ascontiguousarray(D, dtype=np.uint32)
     dd, dD = DeviceBytes.from_numpy(digits), DeviceBytes.from_numpy(D)
     cyc, out = DeviceBytes(8 * 5 * count), DeviceBytes(4 * 32)
-    check(lib().mpres_probe_rounding(nmod, dd.ptr, dD.ptr, count, cyc.ptr, out.ptr, bound_offset, None),
-          "mpres_probe_rounding")
+    check(lib().mpres_probe_rounding(nmod, dd.ptr, dD.ptr, count, cyc.ptr, out.ptr, None), "mpres_probe_rounding")
     torch.cuda.synchronize()
     return cyc.to_numpy(np.int64, 5 * count).reshape(count, 5)
 
