@@ -139,40 +139,6 @@ __global__ void round_parts_probe(const int *digits, const unsigned *D, int coun
     out[lane] = acc;
 }
 
-/* The upward leaf RU(s * recip_ru_i) of the fraction sums, exactly, on the
- * integer pipes: recip_ru_i = R * 2^-83 with a 53-bit R, so s * recip_ru_i is
- * the 84-bit integer P = s * R times 2^-83; rounding it up to 53 significant
- * bits and assembling the double's fields gives the same double __dmul_ru
- * gives (UP = false: truncation, __dmul_rd with recip_rd_i). */
-template <int N, bool UP> __device__ __forceinline__ double int_leaf(uint32_t s, int i) {
-    const Tables<N> &t = T<N>();
-    const uint64_t R = UP ? t.recip_ru_m[i] : t.recip_rd_m[i];
-    const uint64_t lo = (uint64_t)s * (uint32_t)R, hi = (uint64_t)s * (uint32_t)(R >> 32);
-    const uint64_t plo = lo + (hi << 32);
-    const uint64_t phi = (hi >> 32) + (plo < lo);
-    if ((plo | phi) == 0) return 0.0;
-    const int L = phi ? 128 - __clzll((long long)phi) : 64 - __clzll((long long)plo);
-    uint64_t q;
-    bool sticky;
-    if (L > 53) {
-        const int sh = L - 53; /* 1 .. 31 */
-        q = (plo >> sh) | (phi << (64 - sh));
-        sticky = (plo << (64 - sh)) != 0;
-    } else {
-        q = plo << (53 - L);
-        sticky = false;
-    }
-    int e = L - 1 - 83; /* the value is in [2^e, 2^(e+1)) */
-    if (UP && sticky) {
-        q++;
-        if (q >> 53) {
-            q >>= 1;
-            e++;
-        }
-    }
-    return bdbl(((uint64_t)(e + 1023) << 52) | (q & ((1ull << 52) - 1)));
-}
-
 /* cycles of `reps` dependent fraction sums: form 0 = FP64 (the kernels' psum),
  * 1 = fixed point (fixed_eval.cuh), 2 = integer leaves and the FP64 tree */
 template <int N>
@@ -195,7 +161,8 @@ __global__ void psum_probe(const int *digits, int form, int reps, long long *cyc
         } else {
             bits = dbits(psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); }));
         }
-        s[0] ^= (int)(bits & 1); /* the next sum depends on this one */
+#pragma unroll
+        for (int i = 0; i < N; i++) s[i] ^= (int)((bits >> (i % 8)) & 1); /* every leaf of the next sum depends on this one */
         acc += (int)(bits >> 20);
     }
     const long long t1 = clock64();
@@ -231,7 +198,8 @@ __device__ __forceinline__ long long clock_after(uint64_t v, volatile uint64_t *
  * [0] the part_inv products and the upward sum, [1] the number of refinement
  * steps, [2] the final downward sum, [3] the fence overhead of one clock_after;
  * then per refinement step j < 12: [4+3j] ceil(log2) and the row index, [5+3j]
- * the row load and the N modular products, [6+3j] the upward sum. */
+ * the row load and the N modular products, [6+3j] the upward sum (leaves as
+ * the library forms them, int_leaf). */
 template <int N> __global__ void eval_phase_probe(const int *digits, int count, long long *cycles, int *out) {
     const Tables<N> &t = T<N>();
     __shared__ uint64_t sink[32];
@@ -250,7 +218,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
         t0 = t00;
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], t.part_inv[i], i);
-        double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
+        double sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
         sumu = d_frac<true>(sumu);
         long long t1 = clock_after(dbits(sumu), mine);
         c[0] = t1 - t0;
@@ -269,7 +237,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
 #pragma unroll
             for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
             const long long tb = clock_after((uint64_t)s[N - 1] + (uint64_t)s[0], mine);
-            sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
+            sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
             sumu = d_frac<true>(sumu);
             const long long tc = clock_after(dbits(sumu), mine);
             if (it < 12) {
@@ -282,7 +250,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
         }
         c[1] = it;
         const double suml =
-            d_frac<false>(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
+            d_frac<false>(psum<N, false>([&](int i) { return int_leaf<N, false>((uint32_t)s[i], i); }));
         const long long t2 = clock_after(dbits(suml), mine);
         c[2] = t2 - t1;
         acc += (int)(dbits(suml) >> 33);

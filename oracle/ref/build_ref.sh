@@ -2,6 +2,8 @@
 # Builds the reference library's hot path for the CPU, once per moduli set, from
 # the unmodified headers under the reference checkout:
 #   oracle/_ref/libmpres_ref_<N>.so   (N = 8, 16, 32 moduli of 32 bits)
+# and its device code for the GB300, with the constants it computes at start-up:
+#   oracle/_ref/ref_kernels_<N>.cubin, oracle/_ref/ref_consts_<N>.bin
 # Needs the reference sources (REF_SRC, default /root/reference/src) and the
 # GMP/MPFR runtime libraries; the headers for those come from oracle/ref/shim.
 # Test infrastructure only: the output pins the oracle and makes golden vectors.
@@ -41,5 +43,18 @@ for N in ${REF_SETS:-8 16 32}; do
         "$MPFR" "$GMP" &
     pids+=($!)
 done
+# the reference's device code as a cubin for the GB300 (oracle/ref/gpu_harness.cu)
+NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+if [ -x "$NVCC" ]; then
+    for N in ${REF_SETS:-8 16 32}; do
+        PARAMS="$REF_SRC/params/32-bit-moduli/params.${N}_32bit.h"
+        "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 -w \
+            -I"$REF_SRC" -I"$HERE/shim" -include "$PARAMS" \
+            "$HERE/gpu_harness.cu" -o "$OUT/ref_kernels_${N}.cubin" &
+        pids+=($!)
+    done
+fi
 for p in "${pids[@]}"; do wait "$p"; done
+# the device constants the reference computes at start-up, for the cubin
+python3 "$HERE/dump_consts.py" ${REF_SETS:-8 16 32} > /dev/null
 echo "built $(ls "$OUT"/libmpres_ref_*.so | wc -l) reference libraries in $OUT"

@@ -1,0 +1,110 @@
+"""The library against the reference's OWN device code running on the same GPU:
+the reference headers compiled unmodified for sm_103a (oracle/_ref/ref_kernels_<N>.cubin,
+built with the reference checkout by oracle/ref/build_ref.sh) with the constant
+tables its rns_const_init / mp_const_init compute.  Bit-identical results for the
+device arithmetic (cuda::mp_add, mp_mul, mp_mul_d, which carry the rounding, the
+interval evaluation and the power-of-two scaling), for mp_dot, mp_gemm and
+mp_spmv_csr at the reference's launch configurations.  Skipped where the cubin
+was not built (no reference checkout)."""
+import numpy as np
+import pytest
+
+import helpers
+from oracle import ffi, ref_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+def need(n):
+    if not ref_gpu.available(n):
+        pytest.skip("reference cubin for %d moduli not built (no reference checkout)" % n)
+    return ref_gpu.ref_gpu(n)
+
+
+def eq(a, b, what):
+    mm = ffi.mismatches(a, b)
+    assert len(mm) == 0, "%s: %d of %d records differ, first at %d" % (what, len(mm), len(a), mm[0])
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+def test_device_arithmetic_matches_reference_gpu(gpu, n):
+    """Chains of products, sums and products by doubles with exponents over
+    +-60 (roundings of several scaling steps, ambiguous signs), each generation
+    computed by the reference's device functions and by the library from the
+    same operands."""
+    ref = need(n)
+    rng = np.random.default_rng(helpers.SEED + 1900 + n)
+    cnt = 20000
+    pool = gpu.set_d(n, helpers.doubles(rng, cnt, -60, 60))
+    for gen in range(9):
+        i, j = rng.integers(0, len(pool), cnt), rng.integers(0, len(pool), cnt)
+        a, b = pool[i].copy(), pool[j].copy()
+        if gen % 3 == 0:
+            want, got = ref.elementwise("mul", a, b), gpu.elementwise(n, gpu.OP_MUL, a, b)
+        elif gen % 3 == 1:
+            want, got = ref.elementwise("add", a, b), gpu.elementwise(n, gpu.OP_ADD, a, b)
+        else:
+            d = -(1 + np.ldexp(rng.integers(1, 1 << 20, cnt).astype(float), -52 - rng.integers(0, 20, cnt)))
+            want, got = ref.elementwise("mul_d", a, d), gpu.elementwise(n, gpu.OP_MUL_D, a, d)
+        eq(got, want, "generation %d" % gen)
+        pool = np.concatenate([pool, want])[-60000:]
+
+
+@pytest.mark.parametrize("n,count", [(8, 1 << 20), (16, 100003), (32, 30011)])
+def test_dot_matches_reference_gpu(gpu, n, count):
+    """mp_dot at the reference benchmark's order <512,128,8192,256,64>; 2^20
+    elements with 8 moduli is the DOT benchmark."""
+    ref = need(n)
+    import torch
+    rng = np.random.default_rng(helpers.SEED + count + n)
+    mx = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    my = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    x, y = ref_gpu.RefArray(n, count).upload(mx), ref_gpu.RefArray(n, count).upload(my)
+    r, buf = ref_gpu.RefArray(n, 1), ref_gpu.RefArray(n, count)
+    ref.dot(count, x, y, r, buf)
+    ref.sync()
+    want = r.download(mx.dtype)
+    dx, dy, dr = gpu.DeviceArray.from_host(n, mx), gpu.DeviceArray.from_host(n, my), gpu.DeviceArray(n, 1)
+    gpu.dot(n, count, dx, dy, dr, order=(512, 128, 8192, 256, 64))
+    torch.cuda.synchronize()
+    eq(dr.download(), want, "dot")
+
+
+@pytest.mark.parametrize("n,m,cols,k,lo", [(32, 256, 128, 256, -32), (8, 100, 70, 300, -32), (16, 64, 64, 130, -300)])
+def test_gemm_matches_reference_gpu(gpu, n, m, cols, k, lo):
+    ref = need(n)
+    import torch
+    rng = np.random.default_rng(helpers.SEED + 1950 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, lo, -lo))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, lo, -lo))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, lo, -lo))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    rA, rB, rC = (ref_gpu.RefArray(n, len(v)).upload(v) for v in (A, B, C))
+    ral, rbe = ref_gpu.RefArray(n, 1).upload(al), ref_gpu.RefArray(n, 1).upload(be)
+    ref.gemm(m, cols, k, ral, rA, m, rB, k, rbe, rC, m, ref_gpu.RefArray(n, m * cols))
+    ref.sync()
+    want = rC.download(C.dtype)
+    dA, dB, dC = (gpu.DeviceArray.from_host(n, v) for v in (A, B, C))
+    dal, dbe = gpu.DeviceArray.from_host(n, al), gpu.DeviceArray.from_host(n, be)
+    gpu.gemm(n, m, cols, k, dal, dA, m, dB, k, dbe, dC, m)
+    torch.cuda.synchronize()
+    eq(dC.download(), want, "gemm")
+
+
+def test_spmv_csr_matches_reference_gpu(gpu):
+    """2^18 power-law rows (1..1024), 8 moduli."""
+    n = 8
+    ref = need(n)
+    import torch
+    rng = np.random.default_rng(helpers.SEED + 1960)
+    m = 1 << 18
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
+    mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
+    x = gpu.DeviceBytes.from_numpy(mx)
+    y_ref, y_lib = gpu.DeviceBytes(m * mx.dtype.itemsize), gpu.DeviceBytes(m * mx.dtype.itemsize)
+    csr = gpu.DeviceCsr(m, irp, ja, vals)
+    ref.spmv_csr(m, csr.c.irp, csr.c.ja, csr.c.as_, x.ptr, y_ref.ptr)
+    ref.sync()
+    gpu.spmv_csr(n, m, csr, x, y_lib)
+    torch.cuda.synchronize()
+    eq(y_lib.to_numpy(mx.dtype, m), y_ref.to_numpy(mx.dtype, m), "spmv_csr")
