@@ -139,6 +139,45 @@ __global__ void round_parts_probe(const int *digits, const unsigned *D, int coun
     out[lane] = acc;
 }
 
+/* A leaf of the fraction sums, RU(s * recip_ru_i) (UP) or RD(s * recip_rd_i),
+ * exactly, on the integer pipes: recip_i = R * 2^-83 with a 53-bit R, so the
+ * product is the 84-bit integer P = s * R times 2^-83; rounding it to 53
+ * significant bits (up: plus one unit when a dropped bit is set; down:
+ * truncation) and assembling the double's fields gives the double that
+ * __dmul_ru(s, recip_ru_i) / __dmul_rd(s, recip_rd_i) gives.  Measured as an
+ * alternative to the FP64 leaves: the 64-bit integer products and the
+ * normalisation cost more issue slots than the FP64 products they replace
+ * (an 8-leaf upward sum took about 2480 cycles in context against 1250), so
+ * the kernels keep __dmul_ru / __dmul_rd. */
+template <int N, bool UP> __device__ __forceinline__ double int_leaf(uint32_t s, int i) {
+    const Tables<N> &t = T<N>();
+    const uint64_t R = UP ? t.recip_ru_m[i] : t.recip_rd_m[i];
+    const uint64_t lo = (uint64_t)s * (uint32_t)R, hi = (uint64_t)s * (uint32_t)(R >> 32);
+    const uint64_t plo = lo + (hi << 32);
+    const uint64_t phi = (hi >> 32) + (plo < lo);
+    if ((plo | phi) == 0) return 0.0;
+    const int L = phi ? 128 - __clzll((long long)phi) : 64 - __clzll((long long)plo);
+    uint64_t q;
+    bool sticky;
+    if (L > 53) {
+        const int sh = L - 53; /* 1 .. 31 */
+        q = (plo >> sh) | (phi << (64 - sh));
+        sticky = (plo << (64 - sh)) != 0;
+    } else {
+        q = plo << (53 - L);
+        sticky = false;
+    }
+    int e = L - 1 - 83; /* the value is in [2^e, 2^(e+1)) */
+    if (UP && sticky) {
+        q++;
+        if (q >> 53) {
+            q >>= 1;
+            e++;
+        }
+    }
+    return bdbl(((uint64_t)(e + 1023) << 52) | (q & ((1ull << 52) - 1)));
+}
+
 /* cycles of `reps` dependent fraction sums: form 0 = FP64 (the kernels' psum),
  * 1 = fixed point (fixed_eval.cuh), 2 = integer leaves and the FP64 tree */
 template <int N>
@@ -199,7 +238,7 @@ __device__ __forceinline__ long long clock_after(uint64_t v, volatile uint64_t *
  * steps, [2] the final downward sum, [3] the fence overhead of one clock_after;
  * then per refinement step j < 12: [4+3j] ceil(log2) and the row index, [5+3j]
  * the row load and the N modular products, [6+3j] the upward sum (leaves as
- * the library forms them, int_leaf). */
+ * the library forms them, __dmul_ru). */
 template <int N> __global__ void eval_phase_probe(const int *digits, int count, long long *cycles, int *out) {
     const Tables<N> &t = T<N>();
     __shared__ uint64_t sink[32];
@@ -218,7 +257,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
         t0 = t00;
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], t.part_inv[i], i);
-        double sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
+        double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
         sumu = d_frac<true>(sumu);
         long long t1 = clock_after(dbits(sumu), mine);
         c[0] = t1 - t0;
@@ -237,7 +276,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
 #pragma unroll
             for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
             const long long tb = clock_after((uint64_t)s[N - 1] + (uint64_t)s[0], mine);
-            sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
+            sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
             sumu = d_frac<true>(sumu);
             const long long tc = clock_after(dbits(sumu), mine);
             if (it < 12) {
@@ -250,7 +289,7 @@ template <int N> __global__ void eval_phase_probe(const int *digits, int count, 
         }
         c[1] = it;
         const double suml =
-            d_frac<false>(psum<N, false>([&](int i) { return int_leaf<N, false>((uint32_t)s[i], i); }));
+            d_frac<false>(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
         const long long t2 = clock_after(dbits(suml), mine);
         c[2] = t2 - t1;
         acc += (int)(dbits(suml) >> 33);

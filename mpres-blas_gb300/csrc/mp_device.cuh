@@ -329,44 +329,6 @@ __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &
 
 /* ---------------------------- pairwise sums ------------------------------ */
 
-/* A leaf of the fraction sums, RU(s * recip_ru_i) (UP) or RD(s * recip_rd_i),
- * exactly, on the integer pipes: recip_i = R * 2^-83 with a 53-bit R, so the
- * product is the 84-bit integer P = s * R times 2^-83; rounding it to 53
- * significant bits (up: plus one unit when a dropped bit is set; down:
- * truncation) and assembling the double's fields gives the double that
- * __dmul_ru(s, recip_ru_i) / __dmul_rd(s, recip_rd_i) gives.  On GB300 each
- * FP64 warp instruction holds the FP64 pipe of its SM sub-partition for about
- * 64 cycles, and the N leaves are half of a sum's FP64 instructions. */
-template <int N, bool UP> __device__ __forceinline__ double int_leaf(uint32_t s, int i) {
-    const Tables<N> &t = T<N>();
-    const uint64_t R = UP ? t.recip_ru_m[i] : t.recip_rd_m[i];
-    const uint64_t lo = (uint64_t)s * (uint32_t)R, hi = (uint64_t)s * (uint32_t)(R >> 32);
-    const uint64_t plo = lo + (hi << 32);
-    const uint64_t phi = (hi >> 32) + (plo < lo);
-    if ((plo | phi) == 0) return 0.0;
-    const int L = phi ? 128 - __clzll((long long)phi) : 64 - __clzll((long long)plo);
-    uint64_t q;
-    bool sticky;
-    if (L > 53) {
-        const int sh = L - 53; /* 1 .. 31 */
-        q = (plo >> sh) | (phi << (64 - sh));
-        sticky = (plo << (64 - sh)) != 0;
-    } else {
-        q = plo << (53 - L);
-        sticky = false;
-    }
-    int e = L - 1 - 83; /* the value is in [2^e, 2^(e+1)) */
-    if (UP && sticky) {
-        q++;
-        if (q >> 53) {
-            q >>= 1;
-            e++;
-        }
-    }
-    return bdbl(((uint64_t)(e + 1023) << 52) | (q & ((1ull << 52) - 1)));
-}
-
-
 /* The balanced tree of src/pairwise.cuh:855-929 over a power-of-two SPAN with
  * LEN real leaves (missing leaves read 0); leaf(i) is evaluated on demand. */
 template <int SPAN, int LEN, bool UP, class F>
@@ -437,17 +399,40 @@ template <int N> __device__ __forceinline__ int mrc_step(int v, int pivot, int j
  * 8 moduli, 15k for 16, 62k for 32).  Here every finished digit j updates all
  * later digits at once: each digit still takes the steps j = 0 .. i-1 in order,
  * so the values are the same, but the chain is N - 1 rounds of independent
- * products.  Fully unrolled (every index a constant, the digits in registers). */
+ * products.  Up to 16 moduli every index is a constant; for 32 the rounds are
+ * a loop and the next round's finished digit is carried in a scalar, so no
+ * digit is addressed by a runtime index (which would move them to local
+ * memory).  Unrolling the 496 products for 32 moduli as well made the one
+ * warp's mixed-radix digit faster (42k against 104k cycles) but mp_gemm 1024^3
+ * slower (43.0 against 38.2 ms: its kernel, which calls the rounding out of
+ * line, spilled more). */
 template <int N> __device__ __forceinline__ void mrc_digits(int (&v)[N]) {
+    if constexpr (N <= 16) {
 #pragma unroll
-    for (int j = 0; j < N - 1; j++) {
+        for (int j = 0; j < N - 1; j++) {
 #pragma unroll
-        for (int i = j + 1; i < N; i++) v[i] = mrc_step<N>(v[i], v[j], j, i);
+            for (int i = j + 1; i < N; i++) v[i] = mrc_step<N>(v[i], v[j], j, i);
+        }
+    } else {
+        int pivot = v[0];
+#pragma unroll 1
+        for (int j = 0; j < N - 1; j++) {
+            int next = 0;
+#pragma unroll
+            for (int i = 1; i < N; i++) {
+                if (i > j) {
+                    v[i] = mrc_step<N>(v[i], pivot, j, i);
+                    if (i == j + 1) next = v[i];
+                }
+            }
+            pivot = next;
+        }
     }
 }
 
 /* Most significant mixed-radix digit, src/rns.cuh:587-603 (cuda::mrd); out of
- * line so that its N registers of digits do not add to the caller's */
+ * line so that its N registers of digits do not add to the caller's (mp_dot
+ * 2^20 with 8 moduli: 0.82 against 0.92 ms inline) */
 template <int N> __device__ __noinline__ int mrd_digits(const int *x) {
     int v[N];
 #pragma unroll
@@ -522,11 +507,11 @@ __device__ __forceinline__ void eval_refine(int *s, double sumu, er_t &low, er_t
         const int *row = t.pow2 + (size_t)k * N;
 #pragma unroll
         for (int i = 0; i < N; i++) s[i] = mulmod_i<N>(s[i], __ldg(row + i), i);
-        sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
+        sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
         sumu = d_frac<true>(sumu);
         K += k;
     }
-    double suml = psum<N, false>([&](int i) { return int_leaf<N, false>((uint32_t)s[i], i); });
+    double suml = psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); });
     suml = d_frac<false>(suml);
     er_set_d(low, suml);
     er_set_d(upp, sumu);
@@ -572,7 +557,7 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
      * from the refined residues.  Every leaf rounded down is at most the same
      * leaf rounded up, so the lower sum is zero whenever the upper one is, and
      * the reference's test that both are zero is the upper sum's. */
-    double sumu = psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); });
+    double sumu = psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); });
     if (!dnz(sumu)) {
         low.frac = 0.0; low.exp = 0;
         upp.frac = 0.0; upp.exp = 0;
@@ -581,7 +566,7 @@ template <int N> __device__ __forceinline__ void eval_fast(er_t &low, er_t &upp,
     sumu = d_frac<true>(sumu);
     if (dbits(sumu) >= dbits(t.eval_acc)) {
         const double suml =
-            d_frac<false>(psum<N, false>([&](int i) { return int_leaf<N, false>((uint32_t)s[i], i); }));
+            d_frac<false>(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
         er_set_d(low, suml);
         er_set_d(upp, sumu);
         return;
@@ -660,7 +645,7 @@ template <int N> __device__ __forceinline__ int rank_full(const int *x, const in
     return (int)fx_whole(fx_fraction_sum<N, false>(s));
 #else
     const Tables<N> &t = T<N>();
-    return (int)d_trunc_u32(psum<N, false>([&](int i) { return int_leaf<N, false>((uint32_t)s[i], i); }));
+    return (int)d_trunc_u32(psum<N, false>([&](int i) { return __dmul_rd(u31_to_double((uint32_t)s[i]), t.recip_rd[i]); }));
 #endif
 }
 /* cuda::rns_rank_compute_fast, src/rns.cuh:1088-1096: whu.  With mrd(x) = 0,
@@ -676,7 +661,7 @@ template <int N> __device__ __forceinline__ int rank_fast(const int *x, const in
     return (int)fx_whole(fx_fraction_sum<N, true>(s));
 #else
     const Tables<N> &t = T<N>();
-    return (int)d_trunc_u32(psum<N, true>([&](int i) { return int_leaf<N, true>((uint32_t)s[i], i); }));
+    return (int)d_trunc_u32(psum<N, true>([&](int i) { return __dmul_ru(u31_to_double((uint32_t)s[i]), t.recip_ru[i]); }));
 #endif
 }
 

@@ -108,3 +108,89 @@ def test_spmv_csr_matches_reference_gpu(gpu):
     gpu.spmv_csr(n, m, csr, x, y_lib)
     torch.cuda.synchronize()
     eq(y_lib.to_numpy(mx.dtype, m), y_ref.to_numpy(mx.dtype, m), "spmv_csr")
+
+
+def _timed(fn, reps):
+    import time
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    return best * 1e3
+
+
+def test_benchmark_sizes_against_reference_gpu(gpu, oracle, capsys):
+    """The three benchmark workloads run by the reference's own kernels and by the
+    library on the same GPU, same inputs: bit-identical results, and the times of
+    both (best of a few runs, host clock around a synchronised pipeline) printed as
+    one JSON line.  GEMM 1024^3 with 32 moduli, DOT 2^20 with 8, CSR SpMV over
+    2^20 power-law rows with 8."""
+    import json
+    import torch
+    if not all(ref_gpu.available(n) for n in (8, 32)):
+        pytest.skip("reference cubins not built (no reference checkout)")
+    out = {}
+    rng = np.random.default_rng(helpers.SEED + 1)
+    # GEMM
+    n, m = 32, 1024
+    ref = ref_gpu.ref_gpu(n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    B = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    C = gpu.set_d(n, helpers.doubles(rng, m * m, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    rA, rB = ref_gpu.RefArray(n, m * m).upload(A), ref_gpu.RefArray(n, m * m).upload(B)
+    rC, rbuf = ref_gpu.RefArray(n, m * m), ref_gpu.RefArray(n, m * m)
+    ral, rbe = ref_gpu.RefArray(n, 1).upload(al), ref_gpu.RefArray(n, 1).upload(be)
+    rC.upload(C)
+    ref.gemm(m, m, m, ral, rA, m, rB, m, rbe, rC, m, rbuf)
+    ref.sync()
+    want = rC.download(C.dtype)
+    dA, dB, dC = (gpu.DeviceArray.from_host(n, v) for v in (A, B, C))
+    dal, dbe = gpu.DeviceArray.from_host(n, al), gpu.DeviceArray.from_host(n, be)
+    gpu.gemm(n, m, m, m, dal, dA, m, dB, m, dbe, dC, m)
+    torch.cuda.synchronize()
+    eq(dC.download(), want, "gemm 1024^3")
+    out["gemm_1024_32moduli_ms"] = {
+        "reference": _timed(lambda: ref.gemm(m, m, m, ral, rA, m, rB, m, rbe, rC, m, rbuf), 2),
+        "library": _timed(lambda: gpu.gemm(n, m, m, m, dal, dA, m, dB, m, dbe, dC, m), 5)}
+    del rA, rB, rC, rbuf, dA, dB, dC
+    # DOT
+    n, count = 8, 1 << 20
+    ref = ref_gpu.ref_gpu(n)
+    mx = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    my = gpu.set_d(n, helpers.doubles(rng, count, -16, 16))
+    x, y = ref_gpu.RefArray(n, count).upload(mx), ref_gpu.RefArray(n, count).upload(my)
+    r, buf = ref_gpu.RefArray(n, 1), ref_gpu.RefArray(n, count)
+    ref.dot(count, x, y, r, buf)
+    ref.sync()
+    dx, dy, dr = gpu.DeviceArray.from_host(n, mx), gpu.DeviceArray.from_host(n, my), gpu.DeviceArray(n, 1)
+    gpu.dot(n, count, dx, dy, dr)
+    torch.cuda.synchronize()
+    eq(dr.download(), r.download(mx.dtype), "dot 2^20")
+    out["dot_2^20_8moduli_ms"] = {"reference": _timed(lambda: ref.dot(count, x, y, r, buf), 10),
+                                  "library": _timed(lambda: gpu.dot(n, count, dx, dy, dr), 10)}
+    # SpMV
+    rows = 1 << 20
+    irp, ja, vals = helpers.random_csr(rng, rows, rows, helpers.power_law_rows(rng, rows))
+    mxs = gpu.set_d(n, helpers.doubles(rng, rows, -16, 16))
+    xs = gpu.DeviceBytes.from_numpy(mxs)
+    ys_ref, ys_lib = gpu.DeviceBytes(rows * mxs.dtype.itemsize), gpu.DeviceBytes(rows * mxs.dtype.itemsize)
+    csr = gpu.DeviceCsr(rows, irp, ja, vals)
+    run_ref = lambda: ref.spmv_csr(rows, csr.c.irp, csr.c.ja, csr.c.as_, xs.ptr, ys_ref.ptr)  # noqa: E731
+    run_lib = lambda: gpu.spmv_csr(n, rows, csr, xs, ys_lib)  # noqa: E731
+    run_ref()
+    ref.sync()
+    run_lib()
+    torch.cuda.synchronize()
+    eq(ys_lib.to_numpy(mxs.dtype, rows), ys_ref.to_numpy(mxs.dtype, rows), "spmv_csr 2^20 rows")
+    out["spmv_csr_2^20rows_8moduli_ms"] = {"reference": _timed(run_ref, 5), "library": _timed(run_lib, 5)}
+    for v in out.values():
+        v["speedup"] = v["reference"] / v["library"]
+    with capsys.disabled():
+        print("\nREFERENCE_GPU " + json.dumps(out))
