@@ -156,8 +156,14 @@ template <int N> __device__ __forceinline__ void gemv_tile(const GemvOp &g, int 
     }
 }
 
-/* tree over `len` entries of one group (CTA-wide barriers: every thread calls it) */
-template <int N> __device__ __forceinline__ void group_tree(mp_t<N> *s, int lt, int len, bool valid) {
+/* tree over `len` entries of one group (CTA-wide barriers: every thread calls
+ * it); groups that start at a multiple of 32 threads take tree_sum's shuffles
+ * below stride 32 */
+template <int N> __device__ __forceinline__ void group_tree(mp_t<N> *s, int lt, int len, bool valid, bool aligned) {
+    if (aligned) {
+        tree_sum<N>(s, lt, len, valid);
+        return;
+    }
     for (unsigned i = next_pow2((unsigned)len) >> 1; i >= 1; i >>= 1) {
         if (valid && (unsigned)lt < i && (unsigned)lt + i < (unsigned)len) {
             mp_t<N> a = s[lt], b = s[lt + i], r;
@@ -191,7 +197,7 @@ __device__ __forceinline__ void dot_group(const DotOp &d, int dop, int b0, int n
         sdata[t] = acc;
     }
     __syncthreads();
-    group_tree<N>(sdata + grp * b3, lt, b3, valid);
+    group_tree<N>(sdata + grp * b3, lt, b3, valid, (b3 & 31) == 0);
     if (valid && lt == 0) store_aos<N>(sdata[t], parts, d.part_off + blk);
     __threadfence();
     __syncthreads();
@@ -211,7 +217,7 @@ __device__ __forceinline__ void dot_group(const DotOp &d, int dop, int b0, int n
         }
     if (in2) sdata[t] = acc;
     __syncthreads();
-    group_tree<N>(sdata, t, b3, in2);
+    group_tree<N>(sdata, t, b3, in2, true);
     if (t == 0) store_soa<N>(sdata[0], d.rd, d.rs, d.re, d.rv, __ldg(d.rlen), 0);
 }
 

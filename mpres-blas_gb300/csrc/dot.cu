@@ -12,8 +12,9 @@
  * the shape of both trees -- is exactly the reference's for the same
  * (gridDim3, blockDim3), so the result is bit-identical:
  *   pass 1: gridDim3 blocks of blockDim3 threads; thread p accumulates products
- *           p, p + K, p + 2K, ... (K = gridDim3 * blockDim3) from zero, then a
- *           shared-memory tree halving from nextPow2(blockDim3)/2;
+ *           p, p + K, p + 2K, ... (K = gridDim3 * blockDim3) from zero, then the
+ *           tree halving from nextPow2(blockDim3)/2 (shared memory down to
+ *           stride 32, warp shuffles below: tree_sum);
  *   pass 2: one block of blockDim3 threads does the same over the gridDim3
  *           block sums and writes r[0].
  */
@@ -44,18 +45,6 @@ __host__ __device__ inline unsigned next_pow2(unsigned v) {
     return v + 1;
 }
 
-/* shared-memory tree of src/mpreduct.cuh:59-67 over bsize entries */
-template <int N> __device__ __forceinline__ void block_tree(mp_t<N> *sdata, unsigned tid, unsigned bsize) {
-    for (unsigned i = next_pow2(bsize) >> 1; i >= 1; i >>= 1) {
-        if (tid < i && tid + i < bsize) {
-            mp_t<N> a = sdata[tid], b = sdata[tid + i], r;
-            mp_add<N>(r, a, b);
-            sdata[tid] = r;
-        }
-        __syncthreads();
-    }
-}
-
 template <int N, int MAXT>
 __global__ void __launch_bounds__(MAXT) dot_pass1(int n, SoA x, int incx, SoA y, int incy, void *block_sums) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -75,7 +64,7 @@ __global__ void __launch_bounds__(MAXT) dot_pass1(int n, SoA x, int incx, SoA y,
     }
     sdata[tid] = acc;
     __syncthreads();
-    block_tree<N>(sdata, tid, bsize);
+    tree_sum<N>(sdata, (int)tid, (int)bsize, true);
     if (tid == 0) store_aos<N>(sdata[0], block_sums, blockIdx.x);
 }
 
@@ -95,7 +84,7 @@ __global__ void __launch_bounds__(MAXT) dot_pass2(int g3, const void *block_sums
     }
     sdata[tid] = acc;
     __syncthreads();
-    block_tree<N>(sdata, tid, bsize);
+    tree_sum<N>(sdata, (int)tid, (int)bsize, true);
     if (tid == 0) store_soa<N>(sdata[0], rd, rs, re, rv, __ldg(rlen), 0);
 }
 

@@ -1021,6 +1021,56 @@ template <int N> __device__ __forceinline__ void store_aos(const mp_t<N> &v, voi
     p[N / 2 + 4] = v.ev[1].exp;
 }
 
+/* shuffle a whole number down by delta lanes among the lanes of `mask` */
+template <int N> __device__ __forceinline__ mp_t<N> shfl_down(const mp_t<N> &v, int delta, unsigned mask = 0xffffffffu) {
+    mp_t<N> r;
+#pragma unroll
+    for (int i = 0; i < N; i++) r.d[i] = __shfl_down_sync(mask, v.d[i], delta);
+    r.sign = __shfl_down_sync(mask, v.sign, delta);
+    r.exp = __shfl_down_sync(mask, v.exp, delta);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        r.ev[k].frac = __shfl_down_sync(mask, v.ev[k].frac, delta);
+        r.ev[k].exp = __shfl_down_sync(mask, v.ev[k].exp, delta);
+    }
+    return r;
+}
+
+/* The tree of src/mpreduct.cuh:59-67 over the `len` entries s[0 .. len-1] of one
+ * group of threads (lt = the thread's index in the group): for i = nextPow2(len)/2,
+ * ..., 2, 1, entry lt < i with lt + i < len becomes s[lt] + s[lt + i].  Levels
+ * i >= 32 go through shared memory with a barrier each (every thread of the block
+ * calls this); the levels below 32 involve only the group's first 32 entries and
+ * run in the registers of the group's first warp, the partner's sum taken by a
+ * shuffle: the same pairs, added in the same order, without five barriers and
+ * shared-memory round trips.  The group must start at a multiple of 32 threads.
+ * The sum ends in s[0], written by the thread with lt = 0. */
+template <int N> __device__ __forceinline__ void tree_sum(mp_t<N> *s, int lt, int len, bool valid) {
+    unsigned i = len > 1 ? 1u << (31 - __clz(len - 1)) : 0u;
+    for (; i >= 32; i >>= 1) {
+        if (valid && (unsigned)lt < i && (unsigned)lt + i < (unsigned)len) {
+            mp_t<N> a = s[lt], b = s[lt + i], r;
+            mp_add<N>(r, a, b);
+            s[lt] = r;
+        }
+        __syncthreads();
+    }
+    if (valid && lt < 32 && lt < len) {
+        const unsigned mask = len >= 32 ? 0xffffffffu : (1u << len) - 1;
+        mp_t<N> v = s[lt];
+        for (; i >= 1; i >>= 1) {
+            const mp_t<N> o = shfl_down<N>(v, (int)i, mask);
+            if ((unsigned)lt < i && (unsigned)lt + i < (unsigned)len) {
+                mp_t<N> r;
+                mp_add<N>(r, v, o);
+                v = r;
+            }
+        }
+        if (lt == 0) s[0] = v;
+    }
+    __syncthreads();
+}
+
 /* BLAS element index for a stride (negative strides start from the far end) */
 __device__ __forceinline__ long long blas_index(long long i, int n, int inc) {
     return inc > 0 ? i * inc : ((long long)-n + i + 1) * inc;

@@ -130,21 +130,6 @@ __global__ void __launch_bounds__(256) spmv_csr_kernel(int m, const int *__restr
     }
 }
 
-/* shuffle a whole number down by delta lanes */
-template <int N> __device__ __forceinline__ mp_t<N> shfl_down(const mp_t<N> &v, int delta) {
-    mp_t<N> r;
-#pragma unroll
-    for (int i = 0; i < N; i++) r.d[i] = __shfl_down_sync(0xffffffffu, v.d[i], delta);
-    r.sign = __shfl_down_sync(0xffffffffu, v.sign, delta);
-    r.exp = __shfl_down_sync(0xffffffffu, v.exp, delta);
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        r.ev[k].frac = __shfl_down_sync(0xffffffffu, v.ev[k].frac, delta);
-        r.ev[k].exp = __shfl_down_sync(0xffffffffu, v.ev[k].exp, delta);
-    }
-    return r;
-}
-
 template <int N, int TPR>
 __global__ void __launch_bounds__(256) spmv_csrv_kernel(int m, const int *__restrict__ irp, const int *__restrict__ ja,
                                                         const double *__restrict__ as, const void *x, void *y,
