@@ -42,9 +42,14 @@ __device__ __forceinline__ int bucket_of(int len) {
 }
 
 /* Workspace layout (ints): [0, 128) counts, [128, 256) cursors, [256] chunk
- * counter, [257] unused, [512, 512 + m) the sorted row order. */
+ * counter, [257] unused, [258, 260) the total of the row lengths (64-bit),
+ * [260, 512) blocks seen per SM, [512, 512 + m) the sorted row order,
+ * [512 + m, 512 + 2m) ELL row ends. */
+constexpr int kSlots = 252;
 struct Sched {
     int *counts, *cursors, *next, *perm;
+    unsigned long long *total;
+    int *slots, *ends;
 };
 
 /* length of row r: CSR from the row pointers, ELL from its last nonzero slot */
@@ -52,31 +57,43 @@ struct CsrLen {
     const int *irp;
     __device__ int operator()(int r) const { return __ldg(irp + r + 1) - __ldg(irp + r); }
 };
-/* ELL: the first empty slot, found by bisection as if the stored entries of a
- * row formed a prefix (true up to explicit zeros); only the schedule uses it */
-struct EllLen {
-    const double *as;
-    int m, maxnzr;
-    __device__ int operator()(int r) const {
-        int lo = 0, hi = maxnzr;
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (dnz(__ldg(as + (size_t)mid * m + r))) lo = mid + 1;
-            else hi = mid;
-        }
-        return lo;
-    }
+/* ELL: one past the last stored nonzero of the row (ell_row_ends) */
+struct EllEnd {
+    const int *ends;
+    __device__ int operator()(int r) const { return __ldg(ends + r); }
 };
 
 template <class Len> __global__ void bucket_count(int m, Len lenf, Sched s) {
     __shared__ int hist[kBuckets];
+    __shared__ unsigned long long tot;
     for (int b = threadIdx.x; b < kBuckets; b += blockDim.x) hist[b] = 0;
+    if (threadIdx.x == 0) tot = 0;
     __syncthreads();
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
-        atomicAdd(&hist[bucket_of(lenf(r))], 1);
+    unsigned long long mine = 0;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        const int len = lenf(r);
+        atomicAdd(&hist[bucket_of(len)], 1);
+        mine += (unsigned)len;
+    }
+    atomicAdd(&tot, mine);
     __syncthreads();
     for (int b = threadIdx.x; b < kBuckets; b += blockDim.x)
         if (hist[b]) atomicAdd(&s.counts[b], hist[b]);
+    if (threadIdx.x == 0) atomicAdd(s.total, tot);
+}
+
+/* ELL row ends: one past the last nonzero slot of each row (the loop bound of
+ * the row's chain; the reference's kernel visits all maxnzr slots and skips
+ * zeros, src/sparse/spmv/spmv_ell.cuh:50-67, so stopping after the last
+ * nonzero changes nothing).  Consecutive threads take consecutive rows and scan
+ * their slots downwards from maxnzr - 1: each column is one coalesced read of
+ * the warp's 32 rows, and the warp stops at its rows' largest end. */
+__global__ void ell_row_ends(int m, int maxnzr, const double *__restrict__ as, int *ends) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
+        int c = maxnzr;
+        while (c > 0 && !dnz(__ldg(as + (size_t)(c - 1) * m + r))) c--;
+        ends[r] = c;
+    }
 }
 
 /* cursors: exclusive offsets with the longest bucket first (one block) */
@@ -103,6 +120,35 @@ __device__ __forceinline__ int next_chunk(int *next, int size) {
     return __shfl_sync(0xffffffffu, base, 0);
 }
 
+/* Chain-bound schedules.  A lane's time is its rows' chain of dependent
+ * multiple-precision steps, and a warp that shares its SM sub-partition with
+ * others waits for issue slots and the FP64 pipe between its steps.  When the
+ * longest chain (the first row of the sorted order, `tpr` lanes to a row) is at
+ * least the average work of a lane with one block per SM, that chain bounds the
+ * whole call: then only the first block to arrive on each SM works and the
+ * others leave at once, so the longest chains run without neighbours (mp_spmv_csr
+ * over 2^20 power-law rows, 8 moduli: 7.6 ms against 11-13 ms with every block;
+ * the longest chain alone takes 7.3 ms).  Otherwise every block works.  The
+ * blocks share the work through one counter, so how many take part never
+ * changes a result. */
+template <class Len>
+__device__ __forceinline__ bool spare_block(const Sched &s, int m, int sms, int tpr, Len lenf) {
+    __shared__ int spare;
+    if (threadIdx.x == 0) {
+        unsigned smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        const int slot = smid < (unsigned)kSlots ? atomicAdd(s.slots + smid, 1) : 0;
+        bool bound = false;
+        if (m > 0 && slot > 0) {
+            const long long chain = ((long long)lenf(__ldg(s.perm)) + tpr - 1) / tpr;
+            bound = chain * sms * (long long)blockDim.x >= (long long)*s.total;
+        }
+        spare = bound;
+    }
+    __syncthreads();
+    return spare != 0;
+}
+
 template <int N>
 __device__ __forceinline__ void csr_row(int row, const int *__restrict__ irp, const int *__restrict__ ja,
                                         const double *__restrict__ as, const void *x, void *y) {
@@ -122,7 +168,8 @@ __device__ __forceinline__ void csr_row(int row, const int *__restrict__ irp, co
 template <int N>
 __global__ void __launch_bounds__(256) spmv_csr_kernel(int m, const int *__restrict__ irp, const int *__restrict__ ja,
                                                        const double *__restrict__ as, const void *x, void *y,
-                                                       Sched s) {
+                                                       Sched s, int sms) {
+    if (spare_block(s, m, sms, 1, CsrLen{irp})) return;
     const int lane = threadIdx.x & 31;
     for (int base = next_chunk(s.next, 32); base < m; base = next_chunk(s.next, 32)) {
         const int v = base + lane;
@@ -133,7 +180,8 @@ __global__ void __launch_bounds__(256) spmv_csr_kernel(int m, const int *__restr
 template <int N, int TPR>
 __global__ void __launch_bounds__(256) spmv_csrv_kernel(int m, const int *__restrict__ irp, const int *__restrict__ ja,
                                                         const double *__restrict__ as, const void *x, void *y,
-                                                        Sched s) {
+                                                        Sched s, int sms) {
+    if (spare_block(s, m, sms, TPR, CsrLen{irp})) return;
     const int lane = threadIdx.x & 31;
     const int sub = lane & (TPR - 1), group = lane / TPR;
     constexpr int kRows = 32 / TPR;
@@ -169,17 +217,19 @@ __global__ void __launch_bounds__(256) spmv_csrv_kernel(int m, const int *__rest
 }
 
 template <int N>
-__global__ void __launch_bounds__(256) spmv_ell_kernel(int m, int maxnzr, const int *__restrict__ ja,
+__global__ void __launch_bounds__(256) spmv_ell_kernel(int m, const int *__restrict__ ja,
                                                        const double *__restrict__ as, const void *x, void *y,
-                                                       Sched s) {
+                                                       Sched s, int sms) {
+    if (spare_block(s, m, sms, 1, EllEnd{s.ends})) return;
     const int lane = threadIdx.x & 31;
     for (int base = next_chunk(s.next, 32); base < m; base = next_chunk(s.next, 32)) {
         const int v = base + lane;
         if (v < m) {
             const int row = __ldg(s.perm + v);
+            const int end = __ldg(s.ends + row);
             mp_t<N> sum;
             set_zero<N>(sum);
-            for (int col = 0; col < maxnzr; col++) {
+            for (int col = 0; col < end; col++) {
                 const size_t slot = (size_t)col * m + row;
                 const double val = __ldg(as + slot);
                 if (dnz(val)) {
@@ -200,28 +250,44 @@ int grid_for(int work, int threads) {
     return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
 }
 
-/* persistent grid: as many blocks as fit on the current device (computed
- * once per device and kernel) */
-template <class K> int persistent_grid(K kernel, int threads) {
+/* persistent grid: as many blocks as fit on the current device, computed once
+ * per device and kernel (the kernel is the template argument: kernels of one
+ * signature, such as the 8/16/32-moduli instances, must not share a size) */
+template <auto Kernel> int persistent_grid(int threads) {
     static PerDevice<int> grids(positive);
     const int dev = current_device();
     const int g = grids.get(dev, 0, [&] {
         int sms = 0, per_sm = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, threads, 0) != cudaSuccess)
             return 0;
         return sms * (per_sm > 0 ? per_sm : 1);
     });
     return g > 0 ? g : 152;
 }
 
-Sched carve(Workspace ws, int m) {
-    int *w = static_cast<int *>(ws.ptr);
-    return Sched{w, w + kBuckets, w + 2 * kBuckets, w + 512};
+bool positive_int(const int &v) { return v > 0; }
+int sm_count() {
+    static PerDevice<int> sms(positive_int);
+    const int dev = current_device();
+    const int n = sms.get(dev, 0, [&] {
+        int v = 0;
+        return cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess ? v : 0;
+    });
+    return n > 0 ? n : 152;
 }
 
+Sched carve(Workspace ws, int m) {
+    int *w = static_cast<int *>(ws.ptr);
+    return Sched{w, w + kBuckets, w + 2 * kBuckets, w + 512, reinterpret_cast<unsigned long long *>(w + 258),
+                 w + 260, w + 512 + (size_t)m};
+}
+
+/* the workspace header (counts, cursors, counter, total, blocks per SM) is
+ * cleared, the rows counted by length bucket and scattered into the sorted
+ * order */
 template <class Len> cudaError_t sort_rows(int m, Len lenf, Sched sc, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(sc.counts, 0, sizeof(int) * kBuckets, st);
+    cudaError_t e = cudaMemsetAsync(sc.counts, 0, sizeof(int) * 512, st);
     if (e != cudaSuccess) return e;
     bucket_count<<<grid_for(m, 256), 256, 0, st>>>(m, lenf, sc);
     bucket_offsets<<<1, 32, 0, st>>>(sc);
@@ -233,7 +299,8 @@ template <int N> cudaError_t csr(int m, const csr_t &a, const void *x, void *y, 
     Sched sc = carve(ws, m);
     cudaError_t e = sort_rows(m, CsrLen{a.irp}, sc, st);
     if (e != cudaSuccess) return e;
-    spmv_csr_kernel<N><<<persistent_grid(spmv_csr_kernel<N>, 128), 128, 0, st>>>(m, a.irp, a.ja, a.as, x, y, sc);
+    spmv_csr_kernel<N><<<persistent_grid<spmv_csr_kernel<N>>(128), 128, 0, st>>>(m, a.irp, a.ja, a.as, x, y, sc,
+                                                                               sm_count());
     return cudaGetLastError();
 }
 
@@ -242,8 +309,8 @@ cudaError_t csrv_t(int m, const csr_t &a, const void *x, void *y, Workspace ws, 
     Sched sc = carve(ws, m);
     cudaError_t e = sort_rows(m, CsrLen{a.irp}, sc, st);
     if (e != cudaSuccess) return e;
-    spmv_csrv_kernel<N, TPR><<<persistent_grid(spmv_csrv_kernel<N, TPR>, 128), 128, 0, st>>>(m, a.irp, a.ja, a.as,
-                                                                                            x, y, sc);
+    spmv_csrv_kernel<N, TPR><<<persistent_grid<spmv_csrv_kernel<N, TPR>>(128), 128, 0, st>>>(m, a.irp, a.ja, a.as,
+                                                                                            x, y, sc, sm_count());
     return cudaGetLastError();
 }
 
@@ -263,15 +330,16 @@ cudaError_t csrv(int m, int tpr, const csr_t &a, const void *x, void *y, Workspa
 template <int N>
 cudaError_t ell(int m, int maxnzr, const ell_t &a, const void *x, void *y, Workspace ws, cudaStream_t st) {
     Sched sc = carve(ws, m);
-    cudaError_t e = sort_rows(m, EllLen{a.as, m, maxnzr}, sc, st);
+    if (m > 0) ell_row_ends<<<grid_for(m, 256), 256, 0, st>>>(m, maxnzr, a.as, sc.ends);
+    cudaError_t e = sort_rows(m, EllEnd{sc.ends}, sc, st);
     if (e != cudaSuccess) return e;
-    spmv_ell_kernel<N><<<persistent_grid(spmv_ell_kernel<N>, 128), 128, 0, st>>>(m, maxnzr, a.ja, a.as, x, y, sc);
+    spmv_ell_kernel<N><<<persistent_grid<spmv_ell_kernel<N>>(128), 128, 0, st>>>(m, a.ja, a.as, x, y, sc, sm_count());
     return cudaGetLastError();
 }
 
 } // namespace
 
-size_t spmv_workspace_bytes(int m) { return sizeof(int) * ((size_t)m + 512); }
+size_t spmv_workspace_bytes(int m) { return sizeof(int) * (2 * (size_t)m + 512); }
 
 cudaError_t launch_spmv_csr(int nmod, int m, const csr_t &a, const void *x, void *y, Workspace ws, cudaStream_t s) {
     if (ws.bytes < spmv_workspace_bytes(m)) return cudaErrorInvalidValue;

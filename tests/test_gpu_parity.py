@@ -318,6 +318,25 @@ def test_spmv_random_vs_oracle(gpu, oracle, n):
        oracle.spmv_ell(n, small, maxnzr, eja, eas, mx))
 
 
+def test_spmv_short_rows_and_stored_zeros_vs_oracle(gpu, oracle):
+    """2^18 rows of 1..8 entries: the longest chain is below a lane's average
+    work, so every block of the persistent grid takes rows (the power-law cases
+    keep one block per SM).  A fifth of the values are stored zeros, so ELL rows
+    hold zeros before later nonzeros: each row's chain must run to its last
+    nonzero."""
+    n = 8
+    rng = np.random.default_rng(helpers.SEED + 31)
+    m = 1 << 18
+    irp, ja, vals = helpers.random_csr(rng, m, m, rng.integers(1, 9, m))
+    vals[rng.random(len(vals)) < 0.2] = 0.0
+    mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
+    eq(run_spmv(gpu, n, "csr", m, mx, irp, ja, vals), oracle.spmv_csr(n, m, irp, ja, vals, mx))
+    eq(run_spmv(gpu, n, "csrv", m, mx, irp, ja, vals, tpr=4), oracle.spmv_csrv(n, m, 4, irp, ja, vals, mx))
+    maxnzr, eja, eas = helpers.csr_to_ell(m, irp, ja, vals)
+    eq(run_spmv(gpu, n, "ell", m, mx, maxnzr=maxnzr, ell_ja=eja, ell_as=eas),
+       oracle.spmv_ell(n, m, maxnzr, eja, eas, mx))
+
+
 @pytest.fixture(scope="module")
 def spmv_bench_matrix(gpu, oracle):
     """The SpMV benchmark's inputs: 2^20 rows, power-law row lengths 1..1024
