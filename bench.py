@@ -280,7 +280,7 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     per_launch = secs / steps
     achieved = w_int / per_launch
     roof = {"bound": "int", "achieved": achieved / 1e9, "peak": rates["mulmod"] / 1e9, "unit": "Gmulmod/s",
-            "frac": achieved / rates["mulmod"], "traffic": traffic("gemm_nn_lazy"),
+            "frac": achieved / rates["mulmod"], "traffic": traffic("gemm_nn_tiled"),
             "peak_source": "measured in this run: Barrett mulmod microkernel (probe.cu)",
             "work_note": "achieved counts the reference chain's 3*m*n*k*N modular products; the lazy-residue "
                          "chain forms one 64-bit multiply-add per residue and step instead, and the interval "
@@ -1050,6 +1050,8 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="headline GEMM only")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-GEMV and serving workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
+    ap.add_argument("--only", choices=["dot", "spmv"], default=None,
+                    help="one secondary workload alone, its own JSON line (profiling runs)")
     args = ap.parse_args()
     world, rank, local = dist()
 
@@ -1073,6 +1075,12 @@ def main():
     stream = torch.cuda.Stream()
     hbm, peak_src = peaks()
 
+    if args.only:
+        run = bench_dot if args.only == "dot" else bench_spmv
+        r = run(torch, mp, stream, args.steps, max(3, args.warmup), world, hbm)
+        if rank == 0:
+            print(json.dumps({k: v for k, v in r.items() if k != "data"}))
+        return
     g = bench_gemm(torch, mp, stream, args.steps, max(3, args.warmup), world, rank, local)
     extra = {}
     if not args.no_extra:

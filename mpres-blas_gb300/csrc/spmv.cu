@@ -70,10 +70,19 @@ template <class Len> __global__ void bucket_count(int m, Len lenf, Sched s) {
     if (threadIdx.x == 0) tot = 0;
     __syncthreads();
     unsigned long long mine = 0;
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x) {
-        const int len = lenf(r);
-        atomicAdd(&hist[bucket_of(len)], 1);
-        mine += (unsigned)len;
+    const int lane = threadIdx.x & 31;
+    /* warp-uniform trip count; the lanes of one bucket add their count once */
+    for (int r0 = blockIdx.x * blockDim.x; r0 < m; r0 += gridDim.x * blockDim.x) {
+        const int r = r0 + (int)threadIdx.x;
+        const bool ok = r < m;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const int len = lenf(r);
+            const int b = bucket_of(len);
+            const unsigned peers = __match_any_sync(act, b);
+            if (lane == __ffs(peers) - 1) atomicAdd(&hist[b], __popc(peers));
+            mine += (unsigned)len;
+        }
     }
     atomicAdd(&tot, mine);
     __syncthreads();
@@ -108,9 +117,25 @@ __global__ void bucket_offsets(Sched s) {
     }
 }
 
+/* rows into their buckets' ranges of the order; the lanes of a warp that share a
+ * bucket take one cursor increment (row lengths are heavily skewed: on the
+ * power-law matrices nearly half the rows fall into one bucket) */
 template <class Len> __global__ void bucket_scatter(int m, Len lenf, Sched s) {
-    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < m; r += gridDim.x * blockDim.x)
-        s.perm[atomicAdd(&s.cursors[bucket_of(lenf(r))], 1)] = r;
+    const int lane = threadIdx.x & 31;
+    for (int r0 = blockIdx.x * blockDim.x; r0 < m; r0 += gridDim.x * blockDim.x) {
+        const int r = r0 + (int)threadIdx.x;
+        const bool ok = r < m;
+        const unsigned act = __ballot_sync(0xffffffffu, ok);
+        if (ok) {
+            const int b = bucket_of(lenf(r));
+            const unsigned peers = __match_any_sync(act, b);
+            const int leader = __ffs(peers) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&s.cursors[b], __popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            s.perm[base + __popc(peers & ((1u << lane) - 1))] = r;
+        }
+    }
 }
 
 /* a warp's next chunk of `size` entries of the sorted order (-1 when exhausted) */

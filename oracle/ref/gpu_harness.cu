@@ -11,7 +11,8 @@
  * mp_const_init computes, dumped from the CPU build by dump_consts.py).
  *
  * Besides the reference's own __global__ kernels (mp_vector_*, mp_array_reduce_*,
- * matrix_multiply_notrans_kernel, mp_mat*, mp_spmv_csr<32>, ...), three
+ * matrix_multiply_notrans_kernel, mp_mat*, mp_spmv_csr<32>, mp_spmv_csrv<32, tpr>,
+ * mp_spmv_ell<32>, ...), three
  * element-wise entry points apply the reference's device arithmetic to AoS
  * records: r[i] = x[i] + y[i] (cuda::mp_add, src/arith/add.cuh:190-202),
  * x[i] * y[i] (cuda::mp_mul, src/arith/mul.cuh:71-80) and x[i] * d[i]
@@ -32,9 +33,19 @@
 #include "blas/dot.cuh"
 #include "blas/gemm.cuh"
 #include "sparse/spmv/spmv_csr.cuh"
+#include "sparse/spmv/spmv_csrv.cuh"
+#include "sparse/spmv/spmv_ell.cuh"
 
-/* the CSR kernel at the reference benchmark's block size (a template) */
+/* the SpMV kernels at the reference benchmark's block size (templates): CSR,
+ * CSR-vector for every threads-per-row value, ELLPACK */
 template __global__ void cuda::mp_spmv_csr<32>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 1>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 2>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 4>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 8>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 16>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_csrv<32, 32>(const int, const csr_t, mp_float_ptr, mp_float_ptr);
+template __global__ void cuda::mp_spmv_ell<32>(const int, const int, const ell_t, mp_float_ptr, mp_float_ptr);
 
 extern "C" __global__ void ref_ew_add(const mp_float_t *x, const mp_float_t *y, mp_float_t *r, int count) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)

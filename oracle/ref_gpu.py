@@ -10,7 +10,9 @@ templates of its headers, are restated here with the file:line they follow:
 
     dot()   cuda::mp_dot<g1, b1, g2, g3, b3>   src/blas/dot.cuh:85-108 (and mp_array_reduce_sum, :42-66)
     gemm()  cuda::mp_gemm<b1x, b1y, g2x, g2y, b3> src/blas/gemm.cuh:70-168 (no transposition)
-    spmv_csr()  cuda::mp_spmv_csr<32><<<blocks, 32>>>  tests/sparse/spmv/csr/test_mpres_spmv_csr.cuh
+    spmv_csr()  cuda::mp_spmv_csr<32><<<m/32+1, 32>>>  tests/sparse/spmv/csr/test_mpres_spmv_csr.cuh
+    spmv_csrv() cuda::mp_spmv_csrv<32, tpr><<<m/(32/tpr)+1, 32>>>  tests/sparse/spmv/csr/test_mpres_spmv_csrv.cuh:40-65
+    spmv_ell()  cuda::mp_spmv_ell<32><<<m/32+1, 32>>>  tests/sparse/spmv/ell/test_mpres_spmv_ell.cuh:39-62
 
 Numbers travel as AoS mp_float_t records (oracle.ffi.mp_dtype) or SoA mp_array_t
 views of torch tensors (RefArray).
@@ -41,6 +43,8 @@ K = {
     "mat_add_esi": "_ZN4cuda24mp_matrix_add_esi_kernelE10mp_array_tiS0_iS0_iii",
     "mat_add_digits": "_ZN4cuda27mp_matrix_add_digits_kernelE10mp_array_tiS0_iS0_iii",  # internal linkage
     "spmv_csr": "_ZN4cuda11mp_spmv_csrILi32EEEvi5csr_tP10mp_float_tS3_",
+    "spmv_ell": "_ZN4cuda11mp_spmv_ellILi32EEEvii5ell_tP10mp_float_tS3_",
+    **{"spmv_csrv%d" % t: "_ZN4cuda12mp_spmv_csrvILi32ELi%dEEEvi5csr_tP10mp_float_tS3_" % t for t in (1, 2, 4, 8, 16, 32)},
     "ew_add": "ref_ew_add",
     "ew_mul": "ref_ew_mul",
     "ew_mul_d": "ref_ew_mul_d",
@@ -53,6 +57,10 @@ class MpArrayT(ctypes.Structure):
 
 class CsrT(ctypes.Structure):
     _fields_ = [("as_", P), ("ja", P), ("irp", P)]
+
+
+class EllT(ctypes.Structure):
+    _fields_ = [("as_", P), ("ja", P)]
 
 
 def available(n):
@@ -253,3 +261,17 @@ class RefGPU:
         launches it (tests/sparse/spmv/csr/test_mpres_spmv_csr.cuh), device pointers."""
         csr = CsrT(as_ptr, ja_ptr, irp_ptr)
         self.launch("spmv_csr", (m // 32 + 1,), (32,), [ctypes.c_int(m), csr, P(x_ptr), P(y_ptr)], stream=stream)
+
+    def spmv_csrv(self, m, tpr, irp_ptr, ja_ptr, as_ptr, x_ptr, y_ptr, stream=0):
+        """cuda::mp_spmv_csrv<32, tpr><<<m / (32 / tpr) + 1, 32>>>(m, csr, x, y) as the reference's
+        driver launches it (tests/sparse/spmv/csr/test_mpres_spmv_csrv.cuh:40-65)."""
+        csr = CsrT(as_ptr, ja_ptr, irp_ptr)
+        self.launch("spmv_csrv%d" % tpr, (m // (32 // tpr) + 1,), (32,), [ctypes.c_int(m), csr, P(x_ptr), P(y_ptr)],
+                    stream=stream)
+
+    def spmv_ell(self, m, maxnzr, ja_ptr, as_ptr, x_ptr, y_ptr, stream=0):
+        """cuda::mp_spmv_ell<32><<<m / 32 + 1, 32>>>(m, maxnzr, ell, x, y) as the reference's driver
+        launches it (tests/sparse/spmv/ell/test_mpres_spmv_ell.cuh:39-62)."""
+        ell = EllT(as_ptr, ja_ptr)
+        self.launch("spmv_ell", (m // 32 + 1,), (32,), [ctypes.c_int(m), ctypes.c_int(maxnzr), ell, P(x_ptr),
+                                                         P(y_ptr)], stream=stream)

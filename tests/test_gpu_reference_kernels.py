@@ -194,3 +194,57 @@ def test_benchmark_sizes_against_reference_gpu(gpu, oracle, capsys):
         v["speedup"] = v["reference"] / v["library"]
     with capsys.disabled():
         print("\nREFERENCE_GPU " + json.dumps(out))
+
+
+def test_spmv_forms_against_reference_gpu(gpu, capsys):
+    """CSR-vector (tpr 4, 16, 32) and ELL over the SpMV benchmark matrix (2^20
+    power-law rows, 8 moduli) by the reference's own kernels at its drivers'
+    launch shapes and by the library: bit-identical, and both times printed.
+    The ELL slots (12.9 GB) are built on the device from the CSR arrays."""
+    import json
+    import torch
+    n = 8
+    ref = need(n)
+    rng = np.random.default_rng(helpers.SEED + 2)
+    m = 1 << 20
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m))
+    mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
+    rec = mx.dtype.itemsize
+    x = gpu.DeviceBytes.from_numpy(mx)
+    y_ref, y_lib = gpu.DeviceBytes(m * rec), gpu.DeviceBytes(m * rec)
+    csr = gpu.DeviceCsr(m, irp, ja, vals)
+    out = {}
+    for tpr in (4, 16, 32):
+        run_ref = lambda: ref.spmv_csrv(m, tpr, csr.c.irp, csr.c.ja, csr.c.as_, x.ptr, y_ref.ptr)  # noqa: E731
+        run_lib = lambda: gpu.spmv_csrv(n, m, csr, x, y_lib, tpr)  # noqa: E731
+        run_ref()
+        ref.sync()
+        run_lib()
+        torch.cuda.synchronize()
+        eq(y_lib.to_numpy(mx.dtype, m), y_ref.to_numpy(mx.dtype, m), "spmv_csrv tpr %d" % tpr)
+        out["spmv_csrv%d_ms" % tpr] = {"reference": _timed(run_ref, 3), "library": _timed(run_lib, 3)}
+    lens = np.diff(irp).astype(np.int64)
+    maxnzr = int(lens.max())
+    irp_t = torch.from_numpy(irp.astype(np.int64)).cuda()
+    rows = torch.repeat_interleave(torch.arange(m, device="cuda"), torch.from_numpy(lens).cuda())
+    slot = (torch.arange(len(ja), device="cuda") - irp_t[:-1][rows]) * m + rows
+    del rows
+    ell_ja = torch.zeros(maxnzr * m, dtype=torch.int32, device="cuda")
+    ell_as = torch.zeros(maxnzr * m, dtype=torch.float64, device="cuda")
+    ell_ja[slot] = torch.from_numpy(ja.astype(np.int32)).cuda()
+    ell_as[slot] = torch.from_numpy(vals).cuda()
+    del slot, irp_t
+    csr.free()
+    ell = gpu.DeviceEll.from_tensors(m, maxnzr, ell_ja, ell_as)
+    run_ref = lambda: ref.spmv_ell(m, maxnzr, ell_ja.data_ptr(), ell_as.data_ptr(), x.ptr, y_ref.ptr)  # noqa: E731
+    run_lib = lambda: gpu.spmv_ell(n, m, ell, x, y_lib)  # noqa: E731
+    run_ref()
+    ref.sync()
+    run_lib()
+    torch.cuda.synchronize()
+    eq(y_lib.to_numpy(mx.dtype, m), y_ref.to_numpy(mx.dtype, m), "spmv_ell")
+    out["spmv_ell_ms"] = {"reference": _timed(run_ref, 3), "library": _timed(run_lib, 3)}
+    for v in out.values():
+        v["speedup"] = v["reference"] / v["library"]
+    with capsys.disabled():
+        print("\nREFERENCE_GPU_SPMV " + json.dumps(out))
