@@ -11,7 +11,7 @@
  * mp_const_init computes, dumped from the CPU build by dump_consts.py).
  *
  * Besides the reference's own __global__ kernels (mp_vector_*, mp_array_reduce_*,
- * matrix_multiply_notrans_kernel, mp_mat*, mp_spmv_csr<32>, mp_spmv_csrv<32, tpr>,
+ * matrix_multiply_notrans_kernel, matrix_row_sum_kernel, mp_mat*, mp_spmv_csr<32>, mp_spmv_csrv<32, tpr>,
  * mp_spmv_ell<32>, ...), three
  * element-wise entry points apply the reference's device arithmetic to AoS
  * records: r[i] = x[i] + y[i] (cuda::mp_add, src/arith/add.cuh:190-202),
@@ -32,6 +32,7 @@
 #include "kernel_config.cuh"
 #include "blas/dot.cuh"
 #include "blas/gemm.cuh"
+#include "blas/gemv.cuh"
 #include "sparse/spmv/spmv_csr.cuh"
 #include "sparse/spmv/spmv_csrv.cuh"
 #include "sparse/spmv/spmv_ell.cuh"

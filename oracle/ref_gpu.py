@@ -10,6 +10,7 @@ templates of its headers, are restated here with the file:line they follow:
 
     dot()   cuda::mp_dot<g1, b1, g2, g3, b3>   src/blas/dot.cuh:85-108 (and mp_array_reduce_sum, :42-66)
     gemm()  cuda::mp_gemm<b1x, b1y, g2x, g2y, b3> src/blas/gemm.cuh:70-168 (no transposition)
+    gemv()  cuda::mp_gemv<g1, b1, g2, b3>    src/blas/gemv.cuh:150-220 (no transposition, unit strides)
     spmv_csr()  cuda::mp_spmv_csr<32><<<m/32+1, 32>>>  tests/sparse/spmv/csr/test_mpres_spmv_csr.cuh
     spmv_csrv() cuda::mp_spmv_csrv<32, tpr><<<m/(32/tpr)+1, 32>>>  tests/sparse/spmv/csr/test_mpres_spmv_csrv.cuh:40-65
     spmv_ell()  cuda::mp_spmv_ell<32><<<m/32+1, 32>>>  tests/sparse/spmv/ell/test_mpres_spmv_ell.cuh:39-62
@@ -40,6 +41,11 @@ K = {
     "mat2scal_esi": "_ZN4cuda26mp_mat2scal_mul_esi_kernelE10mp_array_tiS0_iS0_ii",
     "mat2scal_digits": "_ZN4cuda29mp_mat2scal_mul_digits_kernelE10mp_array_tiS0_iS0_ii",
     "mat_round": "_ZN4cuda22mp_matrix_round_kernelE10mp_array_tiii",
+    "vec2scal_esi": "_ZN4cuda26mp_vec2scal_mul_esi_kernelE10mp_array_tiS0_iS0_i",
+    "vec2scal_digits": "_ZN4cuda29mp_vec2scal_mul_digits_kernelE10mp_array_tiS0_iS0_i",
+    "mat2vec_esi": "_ZN4cuda32mp_mat2vec_right_scal_esi_kernelE10mp_array_tiS0_iS0_iii",
+    "mat2vec_digits": "_ZN4cuda35mp_mat2vec_right_scal_digits_kernelE10mp_array_tiS0_iS0_iii",  # internal linkage
+    "row_sum": "_ZN4cuda21matrix_row_sum_kernelEjj10mp_array_tS0_ij",  # internal linkage
     "mat_add_esi": "_ZN4cuda24mp_matrix_add_esi_kernelE10mp_array_tiS0_iS0_iii",
     "mat_add_digits": "_ZN4cuda27mp_matrix_add_digits_kernelE10mp_array_tiS0_iS0_iii",  # internal linkage
     "spmv_csr": "_ZN4cuda11mp_spmv_csrILi32EEEvi5csr_tP10mp_float_tS3_",
@@ -100,6 +106,30 @@ class RefArray:
         self.eval.copy_(torch.from_numpy(ev))
         del n
         return self
+
+    @classmethod
+    def copy_of(cls, ta, offset, length):
+        """A RefArray holding elements [offset, offset + length) of an array with the same
+        SoA tensors (digits [size*n], sign, exp [size], eval [2*size, 2]): its own
+        storage, so that its `len` is its length.  The reference's kernels need that:
+        scalar operands are read as eval[0], eval[1] (src/mpvector.cuh:147-148)."""
+        r = cls(ta.nmod, length)
+        n, o = ta.nmod, offset
+        r.digits.copy_(ta.digits[o * n:(o + length) * n])
+        r.sign.copy_(ta.sign[o:o + length])
+        r.exp.copy_(ta.exp[o:o + length])
+        r.eval[:length].copy_(ta.eval[o:o + length])
+        r.eval[length:2 * length].copy_(ta.eval[ta.size + o:ta.size + o + length])
+        return r
+
+    def copy_into(self, ta, offset):
+        """The inverse of copy_of: this array's elements into [offset, offset + size) of ta."""
+        n, o, k = self.n, offset, self.size
+        ta.digits[o * n:(o + k) * n].copy_(self.digits[:k * n])
+        ta.sign[o:o + k].copy_(self.sign[:k])
+        ta.exp[o:o + k].copy_(self.exp[:k])
+        ta.eval[o:o + k].copy_(self.eval[:k])
+        ta.eval[ta.size + o:ta.size + o + k].copy_(self.eval[k:2 * k])
 
     def download(self, dtype):
         out = np.zeros(self.size, dtype)
@@ -255,6 +285,29 @@ class RefGPU:
         self.launch("mat_add_digits", (g2x, g2y), (BLOCK_SIZE_FOR_RESIDUES,),
                     [C.a, i(ldc), C.a, i(ldc), buffer.a, i(m), i(m), i(n)], stream=stream)
         self.launch("mat_round", g3, (16, 16), [C.a, i(ldc), i(m), i(n)], stream=stream)
+
+    def gemv(self, m, n, alpha, A, lda, x, beta, y, buffer1, buffer2, order=(256, 128, 256, 32), stream=0):
+        """cuda::mp_gemv<g1, b1, g2, b3>(mblas_no_trans, m, n, alpha, A, lda, x, 1, beta, y, 1, buffer1,
+        buffer2) (src/blas/gemv.cuh:150-220): buffer1 = alpha*x and y = beta*y (each rounded),
+        buffer2 = A*diag(buffer1) (rounded), then per row the b3-thread sum plus y."""
+        g1, b1, g2, b3 = order
+        i, u = ctypes.c_int, ctypes.c_uint
+        one = i(1)
+        self.launch("vec2scal_esi", (g1,), (b1,), [buffer1.a, one, x.a, one, alpha.a, i(n)], stream=stream)
+        self.launch("vec2scal_digits", (g2,), (BLOCK_SIZE_FOR_RESIDUES,), [buffer1.a, one, x.a, one, alpha.a, i(n)],
+                    stream=stream)
+        self.launch("vec_round", (g1,), (b1,), [buffer1.a, one, i(n)], stream=stream)
+        self.launch("vec2scal_esi", (g1,), (b1,), [y.a, one, y.a, one, beta.a, i(m)], stream=stream)
+        self.launch("vec2scal_digits", (g2,), (BLOCK_SIZE_FOR_RESIDUES,), [y.a, one, y.a, one, beta.a, i(m)],
+                    stream=stream)
+        self.launch("vec_round", (g1,), (b1,), [y.a, one, i(m)], stream=stream)
+        self.launch("mat2vec_esi", (g1, g1), (b1,), [buffer2.a, i(m), A.a, i(lda), buffer1.a, one, i(m), i(n)],
+                    stream=stream)
+        self.launch("mat2vec_digits", (g2, g2), (BLOCK_SIZE_FOR_RESIDUES,),
+                    [buffer2.a, i(m), A.a, i(lda), buffer1.a, one, i(m), i(n)], stream=stream)
+        self.launch("vec_round", (g1,), (b1,), [buffer2.a, one, i(m * n)], stream=stream)
+        self.launch("row_sum", (m,), (b3,), [u(m), u(n), buffer2.a, y.a, one, u(next_pow2(b3))],
+                    smem=b3 * (4 * self.n + 40), stream=stream)
 
     def spmv_csr(self, m, irp_ptr, ja_ptr, as_ptr, x_ptr, y_ptr, stream=0):
         """cuda::mp_spmv_csr<32><<<m / 32 + 1, 32>>>(m, csr, x, y) as the reference's driver

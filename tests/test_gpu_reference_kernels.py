@@ -248,3 +248,114 @@ def test_spmv_forms_against_reference_gpu(gpu, capsys):
         v["speedup"] = v["reference"] / v["library"]
     with capsys.disabled():
         print("\nREFERENCE_GPU_SPMV " + json.dumps(out))
+
+
+@pytest.mark.parametrize("n,m,cols", [(16, 1024, 1024), (8, 300, 77), (32, 64, 200)])
+def test_gemv_matches_reference_gpu(gpu, n, m, cols):
+    """mp_gemv without transposition at the reference benchmark's <256,128,256,32>."""
+    ref = need(n)
+    import torch
+    rng = np.random.default_rng(helpers.SEED + 1970 + n)
+    A = gpu.set_d(n, helpers.doubles(rng, m * cols, -32, 32))
+    x = gpu.set_d(n, helpers.doubles(rng, cols, -32, 32))
+    y = gpu.set_d(n, helpers.doubles(rng, m, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    rA, rx, ry = (ref_gpu.RefArray(n, len(v)).upload(v) for v in (A, x, y))
+    ral, rbe = ref_gpu.RefArray(n, 1).upload(al), ref_gpu.RefArray(n, 1).upload(be)
+    ref.gemv(m, cols, ral, rA, m, rx, rbe, ry, ref_gpu.RefArray(n, cols), ref_gpu.RefArray(n, m * cols))
+    ref.sync()
+    dA, dx, dy = (gpu.DeviceArray.from_host(n, v) for v in (A, x, y))
+    dal, dbe = gpu.DeviceArray.from_host(n, al), gpu.DeviceArray.from_host(n, be)
+    gpu.gemv(n, gpu.NO_TRANS, m, cols, dal, dA, m, dx, dbe, dy, order=(256, 128, 256, 32))
+    torch.cuda.synchronize()
+    eq(dy.download(), ry.download(y.dtype), "gemv")
+
+
+def test_gemv_batch_sample_against_reference_gpu(gpu, capsys):
+    """64 GEMVs of the batched configuration (m, n log-uniform in [32, 4096],
+    entries u*2^e with e in [-32, 32], 16 moduli, NO_TRANS, blockDim3 32): the
+    reference's mp_gemv called once per instance, the library's plain calls and
+    one batched launch, all bit-identical; the three times printed.  Each
+    reference call gets its operands as arrays of their own (copies made outside
+    the timed calls): its kernels read a scalar's upper bound at eval[1]."""
+    import json
+    import time
+    import torch
+    n, count, b3 = 16, 64, 32
+    ref = need(n)
+    sizes = np.exp(np.random.default_rng(helpers.SEED + 1980).uniform(np.log(32), np.log(4096 + 1), (count, 2)))
+    sizes = np.minimum(sizes.astype(np.int64), 4096)
+    M, K = sizes[:, 0], sizes[:, 1]
+    a_off = np.concatenate([[0], np.cumsum(M * K)])
+    x_off = np.concatenate([[0], np.cumsum(K)])
+    y_off = np.concatenate([[0], np.cumsum(M)])
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(helpers.SEED + 1981)
+
+    def fill(arr):
+        u = torch.rand(arr.size, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1
+        e = torch.randint(-32, 33, (arr.size,), generator=gen, device="cuda", dtype=torch.int64)
+        arr.set_d(torch.ldexp(u, e))
+
+    A, X, Y = gpu.TensorArray(n, int(a_off[-1])), gpu.TensorArray(n, int(x_off[-1])), gpu.TensorArray(n, int(y_off[-1]))
+    AB = gpu.TensorArray(n, 2 * count)
+    for arr in (A, X, Y):
+        fill(arr)
+    AB.set_d(torch.rand(2 * count, generator=gen, device="cuda", dtype=torch.float64) * 2 - 1)
+    ops = [(int(M[j]), int(K[j]), AB.view(2 * j, 1), A.view(int(a_off[j]), int(M[j] * K[j])),
+            X.view(int(x_off[j]), int(K[j])), AB.view(2 * j + 1, 1), Y.view(int(y_off[j]), int(M[j])))
+           for j in range(count)]
+    torch.cuda.synchronize()
+    y0 = Y.download()
+
+    # the reference, one call at a time on arrays of their own
+    buf1 = ref_gpu.RefArray(n, int(K.max()))
+    buf2 = ref_gpu.RefArray(n, int((M * K).max()))
+    t_ref = 0.0
+    for j in range(count):
+        m, k = int(M[j]), int(K[j])
+        rA = ref_gpu.RefArray.copy_of(A, int(a_off[j]), m * k)
+        rx = ref_gpu.RefArray.copy_of(X, int(x_off[j]), k)
+        ry = ref_gpu.RefArray.copy_of(Y, int(y_off[j]), m)
+        ral, rbe = ref_gpu.RefArray.copy_of(AB, 2 * j, 1), ref_gpu.RefArray.copy_of(AB, 2 * j + 1, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref.gemv(m, k, ral, rA, m, rx, rbe, ry, buf1, buf2)
+        ref.sync()
+        t_ref += time.perf_counter() - t0
+        ry.copy_into(Y, int(y_off[j]))
+        del rA
+    torch.cuda.synchronize()
+    y_ref = Y.download()
+
+    def run_plain():
+        for m, k, al, Av, xv, be, yv in ops:
+            gpu.gemv(n, gpu.NO_TRANS, m, k, al, Av, m, xv, be, yv, order=(256, 128, 256, b3))
+
+    batch = gpu.Batch(n)
+    for m, k, al, Av, xv, be, yv in ops:
+        batch.add_gemv(gpu.NO_TRANS, m, k, al, Av, m, xv, be, yv, b3=b3)
+    Y.upload(y0)
+    batch.commit(gpu.BATCH_GRAPH | gpu.BATCH_AUTOTUNE)
+    torch.cuda.synchronize()
+
+    def timed_once(fn):
+        Y.upload(y0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) * 1e3, Y.download()
+
+    timed_once(run_plain)
+    t_plain, y_plain = timed_once(run_plain)
+    timed_once(batch.run)
+    t_batch, y_batch = timed_once(batch.run)
+    eq(y_plain, y_ref, "plain calls against the reference")
+    eq(y_batch, y_ref, "batched launch against the reference")
+    batch.destroy()
+    out = {"gemv_x64_16moduli_ms": {"reference": t_ref * 1e3, "library_plain": t_plain, "library_batched": t_batch,
+                                    "speedup_plain": t_ref * 1e3 / t_plain, "speedup_batched": t_ref * 1e3 / t_batch,
+                                    "mp_elements_of_A": int(a_off[-1])}}
+    with capsys.disabled():
+        print("\nREFERENCE_GPU_GEMV " + json.dumps(out))
