@@ -184,6 +184,10 @@ __device__ __forceinline__ void csr_row(int row, const int *__restrict__ irp, co
         mp_t<N> xv, p, s;
         load_aos<N>(xv, x, __ldg(ja + i));
         mp_mul_d<N>(p, xv, __ldg(as + i));
+        if (i == start && zero_add_keeps<N>(p)) { /* the first step adds p to zero */
+            sum = p;
+            continue;
+        }
         mp_add<N>(s, sum, p);
         sum = s;
     }
@@ -216,24 +220,42 @@ __global__ void __launch_bounds__(256) spmv_csrv_kernel(int m, const int *__rest
         const int row = active ? __ldg(s.perm + v) : 0;
         mp_t<N> sum;
         set_zero<N>(sum);
+        bool zero = true; /* sum is still set_zero's zero */
         if (active) {
             const int start = __ldg(irp + row), end = __ldg(irp + row + 1);
             for (int i = start + sub; i < end; i += TPR) {
                 mp_t<N> xv, p, t;
                 load_aos<N>(xv, x, __ldg(ja + i));
                 mp_mul_d<N>(p, xv, __ldg(as + i));
-                mp_add<N>(t, sum, p);
-                sum = t;
+                if (zero && zero_add_keeps<N>(p)) {
+                    sum = p;
+                } else {
+                    mp_add<N>(t, sum, p);
+                    sum = t;
+                }
+                zero = false;
             }
         }
+        /* The tree adds zeros wherever a row has fewer entries than lanes (on
+         * power-law rows most partial sums are zero); additions that
+         * zero_add_keeps shows to return one operand unchanged are skipped. */
 #pragma unroll
         for (int sft = 16; sft >= 1; sft >>= 1) {
             if (TPR >= 2 * sft) {
                 mp_t<N> other = shfl_down<N>(sum, sft);
+                const bool other_zero = __shfl_down_sync(0xffffffffu, zero, sft);
                 if (active && sub < sft) {
-                    mp_t<N> t;
-                    mp_add<N>(t, sum, other);
-                    sum = t;
+                    if (other_zero && (zero || zero_add_keeps<N>(sum))) {
+                        /* sum + 0 = sum */
+                    } else if (zero && zero_add_keeps<N>(other)) {
+                        sum = other;
+                        zero = false;
+                    } else {
+                        mp_t<N> t;
+                        mp_add<N>(t, sum, other);
+                        sum = t;
+                        zero = false;
+                    }
                 }
             }
         }
@@ -254,6 +276,7 @@ __global__ void __launch_bounds__(256) spmv_ell_kernel(int m, const int *__restr
             const int end = __ldg(s.ends + row);
             mp_t<N> sum;
             set_zero<N>(sum);
+            bool zero = true;
             for (int col = 0; col < end; col++) {
                 const size_t slot = (size_t)col * m + row;
                 const double val = __ldg(as + slot);
@@ -261,8 +284,13 @@ __global__ void __launch_bounds__(256) spmv_ell_kernel(int m, const int *__restr
                     mp_t<N> xv, p, t;
                     load_aos<N>(xv, x, __ldg(ja + slot));
                     mp_mul_d<N>(p, xv, val);
-                    mp_add<N>(t, sum, p);
-                    sum = t;
+                    if (zero && zero_add_keeps<N>(p)) {
+                        sum = p;
+                    } else {
+                        mp_add<N>(t, sum, p);
+                        sum = t;
+                    }
+                    zero = false;
                 }
             }
             store_aos<N>(sum, y, row);
