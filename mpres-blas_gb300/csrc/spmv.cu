@@ -180,10 +180,23 @@ __device__ __forceinline__ void csr_row(int row, const int *__restrict__ irp, co
     mp_t<N> sum;
     set_zero<N>(sum);
     const int start = __ldg(irp + row), end = __ldg(irp + row + 1);
+    /* the next entry's x record and value are loaded a step ahead: the gather's
+     * latency overlaps the current step's arithmetic */
+    mp_t<N> xn;
+    double an = 0.0;
+    if (start < end) {
+        load_aos<N>(xn, x, __ldg(ja + start));
+        an = __ldg(as + start);
+    }
     for (int i = start; i < end; i++) {
-        mp_t<N> xv, p, s;
-        load_aos<N>(xv, x, __ldg(ja + i));
-        mp_mul_d<N>(p, xv, __ldg(as + i));
+        const mp_t<N> xv = xn;
+        const double a = an;
+        if (i + 1 < end) {
+            load_aos<N>(xn, x, __ldg(ja + i + 1));
+            an = __ldg(as + i + 1);
+        }
+        mp_t<N> p, s;
+        mp_mul_d<N>(p, xv, a);
         if (i == start && zero_add_keeps<N>(p)) { /* the first step adds p to zero */
             sum = p;
             continue;
@@ -277,12 +290,21 @@ __global__ void __launch_bounds__(256) spmv_ell_kernel(int m, const int *__restr
             mp_t<N> sum;
             set_zero<N>(sum);
             bool zero = true;
+            /* the next slot's value and column are loaded a step ahead (a slot
+             * of another column is another cache line) */
+            double vn = end > 0 ? __ldg(as + row) : 0.0;
+            int jn = end > 0 ? __ldg(ja + row) : 0;
             for (int col = 0; col < end; col++) {
-                const size_t slot = (size_t)col * m + row;
-                const double val = __ldg(as + slot);
+                const double val = vn;
+                const int j = jn;
+                if (col + 1 < end) {
+                    const size_t next = (size_t)(col + 1) * m + row;
+                    vn = __ldg(as + next);
+                    jn = __ldg(ja + next);
+                }
                 if (dnz(val)) {
                     mp_t<N> xv, p, t;
-                    load_aos<N>(xv, x, __ldg(ja + slot));
+                    load_aos<N>(xv, x, j);
                     mp_mul_d<N>(p, xv, val);
                     if (zero && zero_add_keeps<N>(p)) {
                         sum = p;
