@@ -272,9 +272,11 @@ __device__ __forceinline__ void widen32(const Scal32 &x, Scal &y) {
  * each thread then reads its residues one quad at a time (its row's quad and
  * the column's quad, a broadcast) right where they are accumulated.  W(A) is
  * read from L2 once per block instead of once per warp, and only one quad of
- * residues is live at a time: at most 128 registers, so four blocks fit on an
- * SM.  Blocks walk C in groups of kGroupRows row blocks, so the blocks resident
- * at once share their rows of W(A) and columns of W(B) in L2. */
+ * residues is live at a time.  Three blocks an SM (168 registers; mp_gemm
+ * 1024^3 with 32 moduli: 37.8 ms, against 38.3 at four blocks and 128
+ * registers, 44.3 at two; eight k steps a tile 51.3, two 38.5).  Blocks walk C
+ * in groups of kGroupRows row blocks, so the blocks resident at once share
+ * their rows of W(A) and columns of W(B) in L2 (16 rows a group: 38.5 ms). */
 constexpr int kKT = 4;          /* k steps per staged tile */
 constexpr int kGroupRows = 8;   /* row blocks per group of the block order */
 
@@ -343,7 +345,7 @@ __device__ __forceinline__ void stage_tile(GemmTile<N, BX, BY> &tl, int k0, int 
 }
 
 template <int N, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY, 4) gemm_nn_tiled(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
+__global__ void __launch_bounds__(BX *BY, 3) gemm_nn_tiled(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B,
                                                           int ldb, SoA beta, int *cd, int *cs, int *ce, er_t *cv,
                                                           const int *clen, int ldc, const int4 *WA, const int4 *WB) {
     constexpr int Q = N / 4;
