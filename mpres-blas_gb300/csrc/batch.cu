@@ -247,24 +247,39 @@ template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int
         const int row = active ? __ldg(s.perm + first + group) : 0;
         mp_t<N> sum;
         set_zero<N>(sum);
+        bool zero = true; /* sum is still set_zero's zero (see zero_add_keeps) */
         if (active) {
             const int start = __ldg(s.irp + row), end = __ldg(s.irp + row + 1);
             for (int i = start + sub; i < end; i += tpr) {
                 mp_t<N> xv, p, q;
                 load_aos<N>(xv, s.x, __ldg(s.ja + i));
                 mp_mul_d<N>(p, xv, __ldg(s.as + i));
-                mp_add<N>(q, sum, p);
-                sum = q;
+                if (zero && zero_add_keeps<N>(p)) {
+                    sum = p;
+                } else {
+                    mp_add<N>(q, sum, p);
+                    sum = q;
+                }
+                zero = false;
             }
         }
-        /* the fixed tree of src/sparse/spmv/spmv_csrv.cuh:70-84 */
+        /* the fixed tree of src/sparse/spmv/spmv_csrv.cuh:70-84; additions of a
+         * zero that return the other operand unchanged are skipped */
         for (int sft = 16; sft >= 1; sft >>= 1) {
             if (tpr >= 2 * sft) {
                 mp_t<N> other = shfl_down<N>(sum, sft);
+                const bool other_zero = __shfl_down_sync(0xffffffffu, zero, sft);
                 if (active && sub < sft) {
-                    mp_t<N> q;
-                    mp_add<N>(q, sum, other);
-                    sum = q;
+                    if (other_zero && (zero || zero_add_keeps<N>(sum))) {
+                    } else if (zero && zero_add_keeps<N>(other)) {
+                        sum = other;
+                        zero = false;
+                    } else {
+                        mp_t<N> q;
+                        mp_add<N>(q, sum, other);
+                        sum = q;
+                        zero = false;
+                    }
                 }
             }
         }
@@ -275,6 +290,7 @@ template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int
     const int row = __ldg(s.perm + first + t);
     mp_t<N> sum;
     set_zero<N>(sum);
+    bool zero = true;
     if (s.form == kEll) {
         for (int col = 0; col < s.maxnzr; col++) {
             const size_t slot = (size_t)col * s.m + row;
@@ -283,8 +299,13 @@ template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int
                 mp_t<N> xv, p, q;
                 load_aos<N>(xv, s.x, __ldg(s.ja + slot));
                 mp_mul_d<N>(p, xv, val);
-                mp_add<N>(q, sum, p);
-                sum = q;
+                if (zero && zero_add_keeps<N>(p)) {
+                    sum = p;
+                } else {
+                    mp_add<N>(q, sum, p);
+                    sum = q;
+                }
+                zero = false;
             }
         }
     } else {
@@ -293,8 +314,13 @@ template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int
             mp_t<N> xv, p, q;
             load_aos<N>(xv, s.x, __ldg(s.ja + i));
             mp_mul_d<N>(p, xv, __ldg(s.as + i));
-            mp_add<N>(q, sum, p);
-            sum = q;
+            if (zero && zero_add_keeps<N>(p)) {
+                sum = p;
+            } else {
+                mp_add<N>(q, sum, p);
+                sum = q;
+            }
+            zero = false;
         }
     }
     store_aos<N>(sum, s.y, row);
