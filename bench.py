@@ -650,8 +650,7 @@ def bench_batched_gemv(torch, mp, stream, hbm, count=4096, wave_bytes=96 << 30):
             "launches_plain": 2 * count, "bit_identical_all_waves": identical, "shape": info,
             "commit_s": commit_s,
             "roofline": {"bound": "hbm", "achieved": algo / t_batch / 1e9, "peak": hbm, "unit": "GB/s",
-                         "frac": algo / t_batch / 1e9 / hbm, "traffic": traffic("batch_kernel", algo),
-                         "traffic_scope": "all waves, scaled from one ncu capture by algorithmic bytes"},
+                         "frac": algo / t_batch / 1e9 / hbm, "traffic": traffic("batch_kernel", algo)},
             "data": "A, x, y: random draws from 2^23 seeded u*2^e values (e in [-32, 32]) converted on the GPU; "
                     "alpha, beta ~ U(-1, 1)"}
 

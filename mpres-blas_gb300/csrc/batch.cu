@@ -264,7 +264,9 @@ template <int N> __device__ __forceinline__ void spmv_chunk(const SpmvOp &s, int
             }
         }
         /* the fixed tree of src/sparse/spmv/spmv_csrv.cuh:70-84; additions of a
-         * zero that return the other operand unchanged are skipped */
+         * zero that return the other operand unchanged are skipped (a loop, so
+         * that one copy of mp_add serves every level) */
+#pragma unroll 1
         for (int sft = 16; sft >= 1; sft >>= 1) {
             if (tpr >= 2 * sft) {
                 mp_t<N> other = shfl_down<N>(sum, sft);

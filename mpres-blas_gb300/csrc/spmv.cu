@@ -104,6 +104,29 @@ __global__ void ell_row_ends(int m, int maxnzr, const double *__restrict__ as, i
         ends[r] = c;
     }
 }
+/* the same two rows to a thread with 16-byte loads (m even, as 16-byte aligned):
+ * a warp reads 512 contiguous bytes of a column at a time */
+__global__ void ell_row_ends2(int m, int maxnzr, const double *__restrict__ as, int *ends) {
+    const int pairs = m / 2;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < pairs; t += gridDim.x * blockDim.x) {
+        const int r = 2 * t;
+        int c0 = maxnzr, c1 = maxnzr;
+        bool f0 = false, f1 = false;
+        for (int c = maxnzr; c > 0 && !(f0 && f1); c--) {
+            const double2 v = __ldg(reinterpret_cast<const double2 *>(as + (size_t)(c - 1) * m + r));
+            if (!f0) {
+                if (dnz(v.x)) f0 = true;
+                else c0 = c - 1;
+            }
+            if (!f1) {
+                if (dnz(v.y)) f1 = true;
+                else c1 = c - 1;
+            }
+        }
+        ends[r] = c0;
+        ends[r + 1] = c1;
+    }
+}
 
 /* cursors: exclusive offsets with the longest bucket first (one block) */
 __global__ void bucket_offsets(Sched s) {
@@ -251,24 +274,24 @@ __global__ void __launch_bounds__(256) spmv_csrv_kernel(int m, const int *__rest
         }
         /* The tree adds zeros wherever a row has fewer entries than lanes (on
          * power-law rows most partial sums are zero); additions that
-         * zero_add_keeps shows to return one operand unchanged are skipped. */
-#pragma unroll
-        for (int sft = 16; sft >= 1; sft >>= 1) {
-            if (TPR >= 2 * sft) {
-                mp_t<N> other = shfl_down<N>(sum, sft);
-                const bool other_zero = __shfl_down_sync(0xffffffffu, zero, sft);
-                if (active && sub < sft) {
-                    if (other_zero && (zero || zero_add_keeps<N>(sum))) {
-                        /* sum + 0 = sum */
-                    } else if (zero && zero_add_keeps<N>(other)) {
-                        sum = other;
-                        zero = false;
-                    } else {
-                        mp_t<N> t;
-                        mp_add<N>(t, sum, other);
-                        sum = t;
-                        zero = false;
-                    }
+         * zero_add_keeps shows to return one operand unchanged are skipped.  The
+         * levels stay a loop: one copy of mp_add instead of five (unrolled, the
+         * kernel's instruction fetch stalled more than it issued). */
+#pragma unroll 1
+        for (int sft = TPR / 2; sft >= 1; sft >>= 1) {
+            mp_t<N> other = shfl_down<N>(sum, sft);
+            const bool other_zero = __shfl_down_sync(0xffffffffu, zero, sft);
+            if (active && sub < sft) {
+                if (other_zero && (zero || zero_add_keeps<N>(sum))) {
+                    /* sum + 0 = sum */
+                } else if (zero && zero_add_keeps<N>(other)) {
+                    sum = other;
+                    zero = false;
+                } else {
+                    mp_t<N> t;
+                    mp_add<N>(t, sum, other);
+                    sum = t;
+                    zero = false;
                 }
             }
         }
@@ -405,7 +428,10 @@ cudaError_t csrv(int m, int tpr, const csr_t &a, const void *x, void *y, Workspa
 template <int N>
 cudaError_t ell(int m, int maxnzr, const ell_t &a, const void *x, void *y, Workspace ws, cudaStream_t st) {
     Sched sc = carve(ws, m);
-    if (m > 0) ell_row_ends<<<grid_for(m, 256), 256, 0, st>>>(m, maxnzr, a.as, sc.ends);
+    if (m > 0 && (m % 2) == 0 && (reinterpret_cast<uintptr_t>(a.as) % 16) == 0)
+        ell_row_ends2<<<grid_for(m / 2, 256), 256, 0, st>>>(m, maxnzr, a.as, sc.ends);
+    else if (m > 0)
+        ell_row_ends<<<grid_for(m, 256), 256, 0, st>>>(m, maxnzr, a.as, sc.ends);
     cudaError_t e = sort_rows(m, EllEnd{sc.ends}, sc, st);
     if (e != cudaSuccess) return e;
     spmv_ell_kernel<N><<<persistent_grid<spmv_ell_kernel<N>>(128), 128, 0, st>>>(m, a.ja, a.as, x, y, sc, sm_count());

@@ -337,6 +337,20 @@ def test_spmv_short_rows_and_stored_zeros_vs_oracle(gpu, oracle):
        oracle.spmv_ell(n, m, maxnzr, eja, eas, mx))
 
 
+def test_spmv_ell_odd_rows_vs_oracle(gpu, oracle):
+    """ELL with an odd row count (the row-end scan then reads one row per thread
+    instead of two) and stored zeros."""
+    n = 8
+    rng = np.random.default_rng(helpers.SEED + 32)
+    m = 4999
+    irp, ja, vals = helpers.random_csr(rng, m, m, helpers.power_law_rows(rng, m, kmax=64))
+    vals[rng.random(len(vals)) < 0.1] = 0.0
+    mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
+    maxnzr, eja, eas = helpers.csr_to_ell(m, irp, ja, vals)
+    eq(run_spmv(gpu, n, "ell", m, mx, maxnzr=maxnzr, ell_ja=eja, ell_as=eas),
+       oracle.spmv_ell(n, m, maxnzr, eja, eas, mx))
+
+
 @pytest.fixture(scope="module")
 def spmv_bench_matrix(gpu, oracle):
     """The SpMV benchmark's inputs: 2^20 rows, power-law row lengths 1..1024
