@@ -492,7 +492,7 @@ def bench_spmv(torch, mp, stream, steps, warmup, world, hbm, mhz=None):
         r = {"value": world * 2 * nnz / per, "unit": "MP ops/s", "ms_per_step": per * 1e3, "steps": steps,
              "launches": 4 * steps,
              "roofline": {"bound": "hbm", "achieved": a / per / 1e9, "peak": hbm, "unit": "GB/s",
-                          "frac": a / per / 1e9 / hbm, "traffic": traffic(kern) if name in ("csr", "csrv32") else None},
+                          "frac": a / per / 1e9 / hbm, "traffic": traffic(kern) if name in ("csr", "ell") else None},
              "e2e": {"value": world * 2 * nnz * steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": h2d,
                      "d2h_bytes_per_step": m * rec,
                      "matrix": "resident (12.9 GB of slots)" if is_ell else "uploaded every step",
@@ -1049,8 +1049,9 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="headline GEMM only")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-GEMV and serving workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
-    ap.add_argument("--only", choices=["dot", "spmv"], default=None,
-                    help="one secondary workload alone, its own JSON line (profiling runs)")
+    ap.add_argument("--only", choices=["dot", "spmv", "bgemv64"], default=None,
+                    help="one secondary workload alone, its own JSON line (profiling runs; bgemv64: the first 64 "
+                         "instances of the batched GEMV workload)")
     args = ap.parse_args()
     world, rank, local = dist()
 
@@ -1075,8 +1076,11 @@ def main():
     hbm, peak_src = peaks()
 
     if args.only:
-        run = bench_dot if args.only == "dot" else bench_spmv
-        r = run(torch, mp, stream, args.steps, max(3, args.warmup), world, hbm)
+        if args.only == "bgemv64":
+            r = bench_batched_gemv(torch, mp, stream, hbm, count=64)
+        else:
+            run = bench_dot if args.only == "dot" else bench_spmv
+            r = run(torch, mp, stream, args.steps, max(3, args.warmup), world, hbm)
         if rank == 0:
             print(json.dumps({k: v for k, v in r.items() if k != "data"}))
         return
