@@ -314,7 +314,8 @@ __global__ void __launch_bounds__(256) spmv_ell_kernel(int m, const int *__restr
             set_zero<N>(sum);
             bool zero = true;
             /* the next slot's value and column are loaded a step ahead (a slot
-             * of another column is another cache line) */
+             * of another column is another cache line); loading its x record
+             * ahead as well made the call slower (9.6 against 8.9 ms) */
             double vn = end > 0 ? __ldg(as + row) : 0.0;
             int jn = end > 0 ? __ldg(ja + row) : 0;
             for (int col = 0; col < end; col++) {

@@ -347,6 +347,9 @@ def test_spmv_ell_odd_rows_vs_oracle(gpu, oracle):
     vals[rng.random(len(vals)) < 0.1] = 0.0
     mx = gpu.set_d(n, helpers.doubles(rng, m, -16, 16))
     maxnzr, eja, eas = helpers.csr_to_ell(m, irp, ja, vals)
+    # zero slots (padding and stored zeros) carry other, valid columns: never used
+    zero = eas == 0.0
+    eja[zero] = rng.integers(0, m, int(zero.sum()))
     eq(run_spmv(gpu, n, "ell", m, mx, maxnzr=maxnzr, ell_ja=eja, ell_as=eas),
        oracle.spmv_ell(n, m, maxnzr, eja, eas, mx))
 
