@@ -302,7 +302,7 @@ def test_spmv_golden(gpu):
        g["ell"])
 
 
-@pytest.mark.parametrize("n", [8, 16])
+@pytest.mark.parametrize("n", [8, 16, 32])
 def test_spmv_random_vs_oracle(gpu, oracle, n):
     rng = np.random.default_rng(helpers.SEED + 2 + n)
     m = 20000
