@@ -981,9 +981,13 @@ def cpu_spmv_mpfr(irp, ja, vals, xd, budget_s=6.0):
         if t >= budget_s / 2 or rows >= m:
             break
         rows = min(m, rows * 2)
-    return {"value": 2.0 * nnz / t, "unit": "MP ops/s", "cores": L.threads(), "kind": "mpfr",
-            "sample": "reference mpfr_mpspmv_csr loop (MPFR, 120 bits, OpenMP) on the first %d rows (%d nnz), %.1f s"
-                      % (rows, nnz, t)}
+    reps = 1
+    while t < budget_s / 2:  # the whole matrix takes less: repeat it
+        t += L.spmv_csr(rows, sub, ja, vals, xd, ffi.mp_precision(8))[0]
+        reps += 1
+    return {"value": 2.0 * nnz * reps / t, "unit": "MP ops/s", "cores": L.threads(), "kind": "mpfr",
+            "sample": "reference mpfr_mpspmv_csr loop (MPFR, 120 bits, OpenMP) on the first %d rows (%d nnz), "
+                      "%d runs, %.1f s" % (rows, nnz, reps, t)}
 
 
 def cpu_spmv_port(irp, ja, vals, mx, budget_s=6.0):
@@ -1000,8 +1004,14 @@ def cpu_spmv_port(irp, ja, vals, mx, budget_s=6.0):
         if t >= budget_s / 2 or rows >= m:
             break
         rows = min(m, rows * 2)
-    return {"value": 2.0 * nnz / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
-            "sample": "oracle mp_spmv_csr on the first %d rows (%d nnz), %.1f s" % (rows, nnz, t)}
+    reps = 1
+    while t < budget_s / 2:  # the whole matrix takes less: repeat it
+        t0 = time.perf_counter()
+        O.spmv_csr(8, rows, sub, ja, vals, mx)
+        t += time.perf_counter() - t0
+        reps += 1
+    return {"value": 2.0 * nnz * reps / t, "unit": "MP ops/s", "cores": O.threads(), "kind": "port",
+            "sample": "oracle mp_spmv_csr on the first %d rows (%d nnz), %d runs, %.1f s" % (rows, nnz, reps, t)}
 
 
 # -------------------------------------------------------------------- main --
