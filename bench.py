@@ -1059,7 +1059,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true", help="headline GEMM only")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-GEMV and serving workloads")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baselines")
-    ap.add_argument("--only", choices=["dot", "spmv", "bgemv64"], default=None,
+    ap.add_argument("--only", choices=["dot", "spmv", "bgemv64", "bgemm"], default=None,
                     help="one secondary workload alone, its own JSON line (profiling runs; bgemv64: the first 64 "
                          "instances of the batched GEMV workload)")
     args = ap.parse_args()
@@ -1088,6 +1088,8 @@ def main():
     if args.only:
         if args.only == "bgemv64":
             r = bench_batched_gemv(torch, mp, stream, hbm, count=64)
+        elif args.only == "bgemm":
+            r = bench_batched_gemm(torch, mp, stream)
         else:
             run = bench_dot if args.only == "dot" else bench_spmv
             r = run(torch, mp, stream, args.steps, max(3, args.warmup), world, hbm)

@@ -259,76 +259,72 @@ __device__ __forceinline__ void gemm_lazy_output(int m, int k, const MatSoA &alp
     sum.exp = 0;
     sum.ev[0].frac = 0.0; sum.ev[0].exp = 0;
     sum.ev[1].frac = 0.0; sum.ev[1].exp = 0;
-    int since_fold = 0;
-    /* The k chain.  The inner loop runs the steps that stay lazy and leaves at
-     * the first that does not; that step runs out of line, then the loop
-     * resumes.  Keeping the call outside the inner loop keeps the loop free of
-     * the register saves around it (measured 4% of the time at 1024^3). */
-    int i = 0;
-    for (;;) {
-        for (; i < k; i++) {
-            const long long ia = (long long)lda * i + row, ib = (long long)col * ldb + i;
-            int4 u[Q], v[Q];
-#pragma unroll
-            for (int q = 0; q < Q; q++) {
-                u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
-                v[q] = __ldg(wb + (size_t)i * Q + q);
-            }
-            const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
-            const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);
-            const longlong2 a0 = __ldg(aev + ia), a1 = __ldg(aev + lenA + ia);
-            const longlong2 b0 = __ldg(bev + ib), b1 = __ldg(bev + lenB + ib);
-            const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
-            const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
-            /* mp_mul without residues */
-            Scal p;
-            p.sign = sa ^ sb;
-            p.exp = ea + eb;
-            p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
-            p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
-            Scal r;
-            int nzx, nzy;
-            const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
-            const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
-                              small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
-            if (!lazy) break;
-            if (!nzx) {
-#pragma unroll
-                for (int j = 0; j < N; j++) acc[j] = 0;
-            }
-            if (nzy) {
+    /* The k chain, in runs of kFoldEvery steps with one fold of the
+     * accumulators after each (a fold on a step counter inside the loop cost
+     * the tiled kernel 3.5%).  The inner loop runs the steps that stay lazy and
+     * leaves at the first that does not; that step runs out of line, then the
+     * loop resumes.  Keeping the call outside the inner loop keeps the loop free
+     * of the register saves around it (measured 4% of the time at 1024^3). */
+    for (int i0 = 0; i0 < k; i0 += kFoldEvery) {
+        const int i1 = min(i0 + kFoldEvery, k);
+        int i = i0;
+        for (;;) {
+            for (; i < i1; i++) {
+                const long long ia = (long long)lda * i + row, ib = (long long)col * ldb + i;
+                int4 u[Q], v[Q];
 #pragma unroll
                 for (int q = 0; q < Q; q++) {
-                    acc[4 * q] += (uint64_t)(uint32_t)u[q].x * (uint32_t)v[q].x;
-                    acc[4 * q + 1] += (uint64_t)(uint32_t)u[q].y * (uint32_t)v[q].y;
-                    acc[4 * q + 2] += (uint64_t)(uint32_t)u[q].z * (uint32_t)v[q].z;
-                    acc[4 * q + 3] += (uint64_t)(uint32_t)u[q].w * (uint32_t)v[q].w;
+                    u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
+                    v[q] = __ldg(wb + (size_t)i * Q + q);
                 }
+                const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
+                const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);
+                const longlong2 a0 = __ldg(aev + ia), a1 = __ldg(aev + lenA + ia);
+                const longlong2 b0 = __ldg(bev + ib), b1 = __ldg(bev + lenB + ib);
+                const er_t ae0{__longlong_as_double(a0.x), a0.y}, ae1{__longlong_as_double(a1.x), a1.y};
+                const er_t be0{__longlong_as_double(b0.x), b0.y}, be1{__longlong_as_double(b1.x), b1.y};
+                /* mp_mul without residues */
+                Scal p;
+                p.sign = sa ^ sb;
+                p.exp = ea + eb;
+                p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                Scal r;
+                int nzx, nzy;
+                const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
+                const bool lazy = decided && !needs_round<N>(p.ev[1]) && !needs_round<N>(r.ev[1]) &&
+                                  small_exp(ea, 1 << 28) && small_exp(eb, 1 << 28) && small_exp(sum.exp, 1 << 29);
+                if (!lazy) break;
+                if (!nzx) {
+#pragma unroll
+                    for (int j = 0; j < N; j++) acc[j] = 0;
+                }
+                if (nzy) {
+#pragma unroll
+                    for (int q = 0; q < Q; q++) {
+                        acc[4 * q] += (uint64_t)(uint32_t)u[q].x * (uint32_t)v[q].x;
+                        acc[4 * q + 1] += (uint64_t)(uint32_t)u[q].y * (uint32_t)v[q].y;
+                        acc[4 * q + 2] += (uint64_t)(uint32_t)u[q].z * (uint32_t)v[q].z;
+                        acc[4 * q + 3] += (uint64_t)(uint32_t)u[q].w * (uint32_t)v[q].w;
+                    }
+                }
+                sum = r;
             }
-            sum = r;
-            if (++since_fold == kFoldEvery) {
-                since_fold = 0;
+            if (i >= i1) break;
+            {
+                uint64_t w[N]; /* copies: see round_if_needed */
+                Scal sc = sum;
 #pragma unroll
-                for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
+                for (int j = 0; j < N; j++) w[j] = acc[j];
+                full_step<N>(w, &sc, A, (long long)lda * i + row, lenA, B, (long long)col * ldb + i, lenB);
+#pragma unroll
+                for (int j = 0; j < N; j++) acc[j] = w[j];
+                sum = sc;
             }
+            i++;
         }
-        if (i >= k) break;
-        {
-            uint64_t w[N]; /* copies: see round_if_needed */
-            Scal sc = sum;
 #pragma unroll
-            for (int j = 0; j < N; j++) w[j] = acc[j];
-            full_step<N>(w, &sc, A, (long long)lda * i + row, lenA, B, (long long)col * ldb + i, lenB);
-#pragma unroll
-            for (int j = 0; j < N; j++) acc[j] = w[j];
-            sum = sc;
-        }
-        if (++since_fold == kFoldEvery) {
-            since_fold = 0;
-#pragma unroll
-            for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
-        }
-        i++;
+        for (int j = 0; j < N; j++) acc[j] = (acc[j] >> 32) * t.pow2_32[j] + (acc[j] & 0xffffffffull);
     }
     mp_t<N> s;
     {
