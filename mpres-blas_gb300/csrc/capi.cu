@@ -705,7 +705,10 @@ int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_a
      * the workspace cannot grow (same bits, no scratch) */
     const char *no_scratch = std::getenv("MPRES_GEMM_NO_SCRATCH");
     const bool scratch = !(no_scratch && no_scratch[0] == '1');
-    if (scratch && workspace_grow(s, gemm_workspace_bytes(nmod, m, n, k), ws) != cudaSuccess)
+    /* the split form's scratch first (32 moduli), else W(A), W(B) alone */
+    const size_t split = scratch ? gemm_split_workspace_bytes(nmod, m, n, k) : 0;
+    if (scratch && (split == 0 || workspace_grow(s, split, ws) != cudaSuccess) &&
+        workspace_grow(s, gemm_workspace_bytes(nmod, m, n, k), ws) != cudaSuccess)
         ws = Workspace{}; /* no room for W(A), W(B): the step-by-step chain, no scratch */
     cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemm");

@@ -490,12 +490,442 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_tiled(int m, int n, int k, 
     store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
 }
 
+/* ------------------ the split k chain: scalars, then residues -----------------
+ *
+ * The lazy chain of an output is a modular dot product of W(A) and W(B) for its
+ * residues, weighted by the flags of the scalar half, beside a scalar chain
+ * that never looks at the residues as long as every step stays lazy.  When in
+ * addition no step drops an operand (nzx = nzy = 1 after the first step), the
+ * residues are the unweighted sum_i W(A(r,i)) * W(B(i,c)) mod m_j: one modular
+ * matrix product per modulus.  The split form runs the two halves as separate
+ * kernels, each with the registers and schedule its own work wants:
+ *   gemm_scalar_chain   the scalar chain of every output (sign, exponent,
+ *                       interval), no residues: no 64-bit accumulators live in
+ *                       the loop, so more warps share an SM;
+ *   gemm_residue_product  W(A) x W(B) per modulus quad, tiled through shared
+ *                       memory, 64-bit lazy accumulators folded every six
+ *                       steps;
+ *   gemm_split_epilogue the residues of each sum recovered as
+ *                       (-1)^s * W * 2^-e, then alpha*sum, beta*C and the split
+ *                       addition as in the other kernels;
+ *   gemm_redo           outputs whose chain left that form (a step that
+ *                       rounds, an undecided sign, a dropped operand,
+ *                       exponents outside the 32-bit range) run the
+ *                       per-output lazy chain from the start instead.
+ * Every value is the one the single chain computes, so results are the same
+ * bits.  The scratch grows by about the size of C (4N + 48 bytes an output). */
+constexpr int kKT1 = 8;   /* k steps per staged tile of the scalar chain */
+constexpr int kRedo = 2;  /* sign marker: the output runs the per-output chain */
+
+template <int BX, int BY> struct ScalTile {
+    longlong2 aev[kKT1][2][BX];
+    longlong2 bev[kKT1][2][BY];
+    int as[kKT1][BX], ae[kKT1][BX];
+    int bs[kKT1][BY], be[kKT1][BY];
+};
+
+template <int BX, int BY>
+__device__ __forceinline__ void stage_scalars(ScalTile<BX, BY> &tl, int k0, int m, int n, int k, int r0, int c0,
+                                              SoA A, int lda, int lenA, SoA B, int ldb, int lenB) {
+    constexpr int T = BX * BY;
+    const int t = threadIdx.y * BX + threadIdx.x;
+    const longlong2 *aev = reinterpret_cast<const longlong2 *>(A.eval);
+    const longlong2 *bev = reinterpret_cast<const longlong2 *>(B.eval);
+    for (int e = t; e < kKT1 * BX; e += T) {
+        const int r = e % BX, kk = e / BX;
+        const bool ok = (k0 + kk < k) && (r0 + r < m);
+        const long long i = ok ? (long long)lda * (k0 + kk) + r0 + r : 0;
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.as[kk][r]), A.sign + i, ok);
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.ae[kk][r]), A.exp + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.aev[kk][0][r]), aev + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.aev[kk][1][r]), aev + lenA + i, ok);
+    }
+    for (int e = t; e < kKT1 * BY; e += T) {
+        const int kk = e % kKT1, cy = e / kKT1;
+        const bool ok = (k0 + kk < k) && (c0 + cy < n);
+        const long long i = ok ? (long long)ldb * (c0 + cy) + k0 + kk : 0;
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.bs[kk][cy]), B.sign + i, ok);
+        cp_async4((uint32_t)__cvta_generic_to_shared(&tl.be[kk][cy]), B.exp + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.bev[kk][0][cy]), bev + i, ok);
+        cp_async16((uint32_t)__cvta_generic_to_shared(&tl.bev[kk][1][cy]), bev + lenB + i, ok);
+    }
+}
+
+/* what the scalar chain leaves for each output e = col * m + row */
+struct ChainOut {
+    int *sign;   /* the sum's sign, or kRedo */
+    int *exp;
+    er_t *ev;    /* lower bounds of all outputs, then the upper bounds */
+    int2 *redo;  /* (row, col) of the outputs marked kRedo, in no fixed order */
+    int *nredo;
+};
+
+template <int N, int BX, int BY>
+__global__ void __launch_bounds__(BX *BY, 6) gemm_scalar_chain(int m, int n, int k, SoA A, int lda, SoA B, int ldb,
+                                                              ChainOut out) {
+    extern __shared__ __align__(16) unsigned char chain_smem[];
+    ScalTile<BX, BY> *tiles = reinterpret_cast<ScalTile<BX, BY> *>(chain_smem);
+    const Tables<N> &t = T<N>();
+    const int gx = (m + BX - 1) / BX, gy = (n + BY - 1) / BY;
+    const int per_group = kGroupRows * gy;
+    const int grp = blockIdx.x / per_group, in = blockIdx.x % per_group;
+    const int rows_in_group = min(kGroupRows, gx - grp * kGroupRows);
+    const int bx = grp * kGroupRows + in % rows_in_group, by = in / rows_in_group;
+    const int r0 = bx * BX, c0 = by * BY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int row = r0 + tx, col = c0 + ty;
+    const bool live = row < m && col < n;
+    const int lenA = __ldg(A.len), lenB = __ldg(B.len);
+    bool lazy = live;
+    Scal32 s;
+    s.sign = 0;
+    s.exp = 0;
+    s.ev[0].frac = 0.0; s.ev[0].exp = 0;
+    s.ev[1].frac = 0.0; s.ev[1].exp = 0;
+    const int ntiles = (k + kKT1 - 1) / kKT1;
+    stage_scalars<BX, BY>(tiles[0], 0, m, n, k, r0, c0, A, lda, lenA, B, ldb, lenB);
+    cp_async_commit();
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int buf = tile & 1;
+        if (tile + 1 < ntiles)
+            stage_scalars<BX, BY>(tiles[buf ^ 1], (tile + 1) * kKT1, m, n, k, r0, c0, A, lda, lenA, B, ldb, lenB);
+        cp_async_commit();
+        cp_async_wait_one();
+        __syncthreads();
+        const ScalTile<BX, BY> &tl = tiles[buf];
+        const int k0 = tile * kKT1;
+        const int kend = min(kKT1, k - k0);
+        if (lazy) {
+            for (int kk = 0; kk < kend; kk++) {
+                const longlong2 a0 = tl.aev[kk][0][tx], a1 = tl.aev[kk][1][tx];
+                const longlong2 b0 = tl.bev[kk][0][ty], b1 = tl.bev[kk][1][ty];
+                const int sa = tl.as[kk][tx], ea = tl.ae[kk][tx], sb = tl.bs[kk][ty], eb = tl.be[kk][ty];
+                if (!(fits32(ea, kExp32 / 2) && fits32(eb, kExp32 / 2) && fits32(a0.y, kExp32) &&
+                      fits32(a1.y, kExp32) && fits32(b0.y, kExp32) && fits32(b1.y, kExp32) &&
+                      fits32(s.exp, kExp32) && fits32(s.ev[0].exp, kExp32) && fits32(s.ev[1].exp, kExp32))) {
+                    lazy = false;
+                    break;
+                }
+                const er32 ae0{__longlong_as_double(a0.x), (int)a0.y}, ae1{__longlong_as_double(a1.x), (int)a1.y};
+                const er32 be0{__longlong_as_double(b0.x), (int)b0.y}, be1{__longlong_as_double(b1.x), (int)b1.y};
+                Scal32 p;
+                p.sign = sa ^ sb;
+                p.exp = ea + eb;
+                p.ev[0] = er_md32<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                p.ev[1] = er_md32<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                Scal32 r;
+                int nzx, nzy;
+                const bool decided = add_scalars32<N>(r, nzx, nzy, s, p);
+                /* the first step adds to zero: dropping that zero changes no residue */
+                if (!decided || needs_round32<N>(p.ev[1]) || needs_round32<N>(r.ev[1]) || !nzy ||
+                    (!nzx && k0 + kk > 0)) {
+                    lazy = false;
+                    break;
+                }
+                s = r;
+            }
+        }
+        __syncthreads(); /* the buffer is restaged by the next iteration */
+    }
+    cp_async_wait_all();
+    /* every thread of the warp (BX = 32 lanes of one row block) arrives here */
+    const unsigned redo = __ballot_sync(0xffffffffu, live && !lazy);
+    if (live) {
+        const size_t e = (size_t)col * m + row, mn = (size_t)m * n;
+        if (lazy) {
+            out.sign[e] = s.sign;
+            out.exp[e] = s.exp;
+            out.ev[e] = er_t{s.ev[0].frac, s.ev[0].exp};
+            out.ev[mn + e] = er_t{s.ev[1].frac, s.ev[1].exp};
+        } else {
+            out.sign[e] = kRedo;
+        }
+    }
+    if (redo) {
+        const int lane = tx & 31;
+        int base = 0;
+        if (lane == __ffs(redo) - 1) base = atomicAdd(out.nredo, __popc(redo));
+        base = __shfl_sync(0xffffffffu, base, __ffs(redo) - 1);
+        if (live && !lazy) out.redo[base + __popc(redo & ((1u << lane) - 1u))] = make_int2(row, col);
+    }
+}
+
+/* W(B) of a k x n matrix as int4 [k][N/4][n]: consecutive threads take
+ * consecutive columns, so the stores of a warp are contiguous */
+template <int N>
+__global__ void __launch_bounds__(256) gemm_prescale_kq(const int *digits, const int *sign, const int *exp, int ld,
+                                                        int k, int n, int4 *out) {
+    constexpr int Q = N / 4;
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (long long)k * n) return;
+    const int r = (int)(e / n), c = (int)(e % n);
+    const long long src = (long long)ld * c + r;
+    const int sg = __ldg(sign + src), x = __ldg(exp + src);
+    const int4 *dp = reinterpret_cast<const int4 *>(digits + (size_t)src * N);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int4 d = __ldg(dp + q);
+        int4 w;
+        w.x = (int)encode_residue<N>(d.x, sg, x, 4 * q);
+        w.y = (int)encode_residue<N>(d.y, sg, x, 4 * q + 1);
+        w.z = (int)encode_residue<N>(d.z, sg, x, 4 * q + 2);
+        w.w = (int)encode_residue<N>(d.w, sg, x, 4 * q + 3);
+        out[((size_t)r * Q + q) * n + c] = w;
+    }
+}
+
+/* S = W(A) x W(B) mod m_j for the four moduli of quad blockIdx.y: a block
+ * computes a kRT x kCT tile of S, lane l of warp w the rows l and l + 32 and
+ * the columns 4w .. 4w + 3 (32 accumulators of 64 bits); the k tiles of W(A)
+ * (kRT int4 a step) and W(B) (kCT int4) are staged by cp.async, double
+ * buffered.  A product is below m^2 < 2^60.6 and a folded accumulator below
+ * 2^62.3, so six products go between folds.  The result, reduced, goes to
+ * int4 [n][N/4][m]. */
+constexpr int kRT = 64, kCT = 32, kKT2 = 12;
+static_assert(kKT2 == 2 * kFoldEvery, "two folds per k tile");
+
+template <int N>
+__global__ void __launch_bounds__(256) gemm_residue_product(int m, int n, int k, const int4 *WA, const int4 *WB,
+                                                           int4 *WS) {
+    constexpr int Q = N / 4;
+    __shared__ __align__(16) int4 sa[2][kKT2][kRT];
+    __shared__ __align__(16) int4 sb[2][kKT2][kCT];
+    const Tables<N> &t = T<N>();
+    const int q = blockIdx.y;
+    const int gx = (m + kRT - 1) / kRT;
+    const int r0 = (blockIdx.x % gx) * kRT, c0 = (blockIdx.x / gx) * kCT;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t c32[4], mods[4], mus[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        c32[j] = t.pow2_32[4 * q + j];
+        mods[j] = (uint32_t)t.moduli[4 * q + j];
+        mus[j] = t.mu[4 * q + j];
+    }
+    uint64_t acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+#pragma unroll
+            for (int x = 0; x < 4; x++) acc[i][j][x] = 0;
+    auto stage = [&](int buf, int k0) {
+        for (int e = threadIdx.x; e < kKT2 * kRT; e += 256) {
+            const int kk = e / kRT, r = e % kRT;
+            const bool ok = (k0 + kk < k) && (r0 + r < m);
+            const int4 *src = ok ? WA + ((size_t)(k0 + kk) * Q + q) * m + r0 + r : WA;
+            cp_async16((uint32_t)__cvta_generic_to_shared(&sa[buf][kk][r]), src, ok);
+        }
+        for (int e = threadIdx.x; e < kKT2 * kCT; e += 256) {
+            const int kk = e / kCT, c = e % kCT;
+            const bool ok = (k0 + kk < k) && (c0 + c < n);
+            const int4 *src = ok ? WB + ((size_t)(k0 + kk) * Q + q) * n + c0 + c : WB;
+            cp_async16((uint32_t)__cvta_generic_to_shared(&sb[buf][kk][c]), src, ok);
+        }
+    };
+    const int ntiles = (k + kKT2 - 1) / kKT2;
+    stage(0, 0);
+    cp_async_commit();
+    for (int tile = 0; tile < ntiles; tile++) {
+        const int buf = tile & 1;
+        if (tile + 1 < ntiles) stage(buf ^ 1, (tile + 1) * kKT2);
+        cp_async_commit();
+        cp_async_wait_one();
+        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            /* staged zeros past k add nothing, so every tile runs its full length */
+#pragma unroll
+            for (int kk = h * kFoldEvery; kk < (h + 1) * kFoldEvery; kk++) {
+                const int4 a0 = sa[buf][kk][lane], a1 = sa[buf][kk][lane + 32];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int4 b = sb[buf][kk][4 * w + j];
+                    acc[0][j][0] += (uint64_t)(uint32_t)a0.x * (uint32_t)b.x;
+                    acc[0][j][1] += (uint64_t)(uint32_t)a0.y * (uint32_t)b.y;
+                    acc[0][j][2] += (uint64_t)(uint32_t)a0.z * (uint32_t)b.z;
+                    acc[0][j][3] += (uint64_t)(uint32_t)a0.w * (uint32_t)b.w;
+                    acc[1][j][0] += (uint64_t)(uint32_t)a1.x * (uint32_t)b.x;
+                    acc[1][j][1] += (uint64_t)(uint32_t)a1.y * (uint32_t)b.y;
+                    acc[1][j][2] += (uint64_t)(uint32_t)a1.z * (uint32_t)b.z;
+                    acc[1][j][3] += (uint64_t)(uint32_t)a1.w * (uint32_t)b.w;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 2; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int x = 0; x < 4; x++)
+                        acc[i][j][x] = (acc[i][j][x] >> 32) * c32[x] + (acc[i][j][x] & 0xffffffffull);
+        }
+        __syncthreads(); /* the buffer is restaged by the next iteration */
+    }
+    cp_async_wait_all();
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const int r = r0 + lane + 32 * i;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int c = c0 + 4 * w + j;
+            if (r < m && c < n) {
+                int4 o;
+                o.x = (int)reduce64(acc[i][j][0], mods[0], mus[0], c32[0]);
+                o.y = (int)reduce64(acc[i][j][1], mods[1], mus[1], c32[1]);
+                o.z = (int)reduce64(acc[i][j][2], mods[2], mus[2], c32[2]);
+                o.w = (int)reduce64(acc[i][j][3], mods[3], mus[3], c32[3]);
+                WS[((size_t)c * Q + q) * m + r] = o;
+            }
+        }
+    }
+}
+
+/* the outputs whose chain stayed in the split form: residues of the sum from
+ * the modular product, then the epilogue of the other kernels */
+template <int N>
+__global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alpha, SoA beta, int *cd, int *cs,
+                                                           int *ce, er_t *cv, const int *clen, int ldc,
+                                                           const int4 *WS, ChainOut in) {
+    constexpr int Q = N / 4;
+    const Tables<N> &t = T<N>();
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long mn = (long long)m * n;
+    if (e >= mn) return;
+    const int sg = in.sign[e];
+    if (sg == kRedo) return;
+    const int row = (int)(e % m), col = (int)(e / m);
+    mp_t<N> s;
+    s.sign = sg;
+    s.exp = in.exp[e];
+    s.ev[0] = in.ev[e];
+    s.ev[1] = in.ev[mn + e];
+    const int4 *ws = WS + (size_t)col * Q * m + row;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int4 v = __ldg(ws + (size_t)q * m);
+        const uint32_t vv[4] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int i = 4 * q + j;
+            const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
+            const uint32_t d = mulmod(vv[j], pow2mod(-(long long)s.exp, md, mu), md, mu);
+            s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
+        }
+    }
+    const int lenC = __ldg(clen);
+    const long long ic = (long long)col * ldc + row;
+    mp_t<N> al, be, buf, c0v, cb, res;
+    load_soa<N>(al, alpha.digits, alpha.sign, alpha.exp, alpha.eval, __ldg(alpha.len), 0);
+    load_soa<N>(be, beta.digits, beta.sign, beta.exp, beta.eval, __ldg(beta.len), 0);
+    mp_mul<N>(buf, s, al);
+    load_soa<N>(c0v, cd, cs, ce, cv, lenC, ic);
+    mp_mul<N>(cb, c0v, be);
+    split_add<N>(res, cb, buf);
+    store_soa<N>(res, cd, cs, ce, cv, lenC, ic);
+}
+
+/* the outputs marked kRedo: the per-output lazy chain and its epilogue */
+template <int N>
+__global__ void __launch_bounds__(128, 3) gemm_redo(int m, int n, int k, SoA alpha, SoA A, int lda, SoA B, int ldb,
+                                                    SoA beta, int *cd, int *cs, int *ce, er_t *cv, const int *clen,
+                                                    int ldc, const int4 *WA, const int4 *WB, ChainOut in) {
+    const int count = *in.nredo;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const int2 rc = in.redo[i];
+        gemm_lazy_output<N, true>(m, k, alpha, A, lda, B, ldb, beta, cd, cs, ce, cv, clen, ldc, WA, WB, rc.x, rc.y,
+                                  n);
+    }
+}
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+/* the split form's scratch, carved in this order */
+struct SplitScratch {
+    int4 *wa, *wb, *ws;
+    ChainOut out;
+};
+size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp) {
+    const size_t mn = (size_t)m * n;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off = align256(off + bytes);
+        return at;
+    };
+    const size_t wa = take((size_t)m * k * nmod * 4);
+    const size_t wb = take((size_t)k * n * nmod * 4);
+    const size_t ws = take(mn * nmod * 4);
+    const size_t sg = take(mn * 4);
+    const size_t ex = take(mn * 4);
+    const size_t ev = take(mn * 2 * sizeof(er_t));
+    const size_t rd = take(mn * sizeof(int2));
+    const size_t nr = take(sizeof(int));
+    if (sp) {
+        char *p = static_cast<char *>(base);
+        sp->wa = reinterpret_cast<int4 *>(p + wa);
+        sp->wb = reinterpret_cast<int4 *>(p + wb);
+        sp->ws = reinterpret_cast<int4 *>(p + ws);
+        sp->out = ChainOut{reinterpret_cast<int *>(p + sg), reinterpret_cast<int *>(p + ex),
+                           reinterpret_cast<er_t *>(p + ev), reinterpret_cast<int2 *>(p + rd),
+                           reinterpret_cast<int *>(p + nr)};
+    }
+    return off;
+}
+
+template <int N>
+cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
+                      const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
+                      Workspace ws, cudaStream_t s) {
+    constexpr int BX = 32, BY = 4;
+    SplitScratch sp;
+    split_scratch(N, m, n, k, ws.ptr, &sp);
+    const long long na = (long long)m * k, nb = (long long)k * n, mn = (long long)m * n;
+    const long long gx = (m + BX - 1) / BX, gy = (n + BY - 1) / BY;
+    const long long rt = ((long long)m + kRT - 1) / kRT, ct = ((long long)n + kCT - 1) / kCT;
+    if (gx * gy > (1ll << 28) || rt * ct > (1ll << 30) || mn >= (1ll << 31)) return cudaErrorInvalidConfiguration;
+    constexpr size_t smem = 2 * sizeof(ScalTile<BX, BY>);
+    static PerDevice<cudaError_t> attrs(cuda_ok);
+    const int dev = current_device();
+    cudaError_t e = attrs.get(dev, cudaErrorInvalidDevice, [] {
+        return cudaFuncSetAttribute(gemm_scalar_chain<N, BX, BY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem);
+    });
+    if (e != cudaSuccess) return e;
+    static PerDevice<int> redo_grid([](const int &g) { return g > 0; });
+    const int rgrid = redo_grid.get(dev, 0, [dev] {
+        int sms = 0, per = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gemm_redo<N>, 128, 0) != cudaSuccess)
+            return 0;
+        return sms * (per > 0 ? per : 1);
+    });
+    if (rgrid <= 0) return cudaErrorInvalidDevice;
+    if ((e = cudaMemsetAsync(sp.out.nredo, 0, sizeof(int), s)) != cudaSuccess) return e;
+    gemm_prescale<N, true><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A.digits, A.sign, A.exp, lda, m, k, sp.wa);
+    gemm_prescale_kq<N><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, sp.wb);
+    gemm_scalar_chain<N, BX, BY><<<(unsigned)(gx * gy), dim3(BX, BY), smem, s>>>(m, n, k, soa(A), lda, soa(B), ldb,
+                                                                              sp.out);
+    gemm_residue_product<N><<<dim3((unsigned)(rt * ct), N / 4), 256, 0, s>>>(m, n, k, sp.wa, sp.wb, sp.ws);
+    er_t *cv = reinterpret_cast<er_t *>(C.eval);
+    gemm_split_epilogue<N><<<(unsigned)((mn + 127) / 128), 128, 0, s>>>(m, n, soa(alpha), soa(beta), C.digits, C.sign,
+                                                                         C.exp, cv, C.len, ldc, sp.ws, sp.out);
+    const long long want = (mn + 127) / 128;
+    gemm_redo<N><<<(unsigned)(want < rgrid ? want : rgrid), 128, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B),
+                                                                         ldb, soa(beta), C.digits, C.sign, C.exp, cv,
+                                                                         C.len, ldc, sp.wa, sp.wb, sp.out);
+    return cudaGetLastError();
+}
+
 template <int N>
 cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda, const mp_array_t &B,
                 int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s) {
     constexpr int BX = 32, BY = 4;
     dim3 block(BX, BY), grid((m + BX - 1) / BX, (n + BY - 1) / BY);
     er_t *cv = reinterpret_cast<er_t *>(C.eval);
+    if constexpr (N == 32) {
+        if (ws.ptr != nullptr && ws.bytes >= gemm_split_workspace_bytes(N, m, n, k))
+            return run_split<N>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s);
+    }
     if (ws.ptr != nullptr && ws.bytes >= gemm_workspace_bytes(N, m, n, k)) {
         int4 *wa = static_cast<int4 *>(ws.ptr);
         int4 *wb = wa + (size_t)m * k * (N / 4);
@@ -526,6 +956,11 @@ cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &
 
 size_t gemm_workspace_bytes(int nmod, int m, int n, int k) {
     return ((size_t)m * k + (size_t)k * n) * (size_t)nmod * 4;
+}
+
+size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k) {
+    if (nmod != 32) return 0;
+    return split_scratch(nmod, m, n, k, nullptr, nullptr);
 }
 
 cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,

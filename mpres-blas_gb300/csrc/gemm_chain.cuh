@@ -238,19 +238,22 @@ constexpr int kFoldEvery = 6;
 
 /* One output C(row, col) of C = alpha*A*B + beta*C with the lazy-residue k
  * chain (per-thread loads of W(A), W(B) and of the A and B scalars), then the
- * epilogue: alpha*sum, beta*C and the split addition. */
-template <int N>
+ * epilogue: alpha*sum, beta*C and the split addition.  W(A) is int4
+ * [k][N/4][m]; W(B) is int4 [n][k][N/4], or with B_KQN int4 [k][N/4][n] (n
+ * given), the layout of the split chain's modular product. */
+template <int N, bool B_KQN = false>
 __device__ __forceinline__ void gemm_lazy_output(int m, int k, const MatSoA &alpha, const MatSoA &A, int lda,
                                                  const MatSoA &B, int ldb, const MatSoA &beta, int *cd, int *cs,
                                                  int *ce, er_t *cv, const int *clen, int ldc, const int4 *WA,
-                                                 const int4 *WB, int row, int col) {
+                                                 const int4 *WB, int row, int col, int n = 0) {
     constexpr int Q = N / 4;
     const Tables<N> &t = T<N>();
     const int lenA = __ldg(A.len), lenB = __ldg(B.len);
     const longlong2 *aev = reinterpret_cast<const longlong2 *>(A.eval);
     const longlong2 *bev = reinterpret_cast<const longlong2 *>(B.eval);
     const int4 *wa = WA + row;
-    const int4 *wb = WB + (size_t)col * k * Q;
+    const int4 *wb = B_KQN ? WB + col : WB + (size_t)col * k * Q;
+    const size_t wb_k = B_KQN ? (size_t)Q * n : (size_t)Q, wb_q = B_KQN ? (size_t)n : 1;
     uint64_t acc[N];
 #pragma unroll
     for (int i = 0; i < N; i++) acc[i] = 0;
@@ -275,7 +278,7 @@ __device__ __forceinline__ void gemm_lazy_output(int m, int k, const MatSoA &alp
 #pragma unroll
                 for (int q = 0; q < Q; q++) {
                     u[q] = __ldg(wa + ((size_t)i * Q + q) * m);
-                    v[q] = __ldg(wb + (size_t)i * Q + q);
+                    v[q] = __ldg(wb + (size_t)i * wb_k + q * wb_q);
                 }
                 const int sa = __ldg(A.sign + ia), ea = __ldg(A.exp + ia);
                 const int sb = __ldg(B.sign + ib), eb = __ldg(B.exp + ib);

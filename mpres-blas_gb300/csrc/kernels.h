@@ -52,6 +52,10 @@ cudaError_t launch_gemv(int nmod, bool trans, int m, int n, const mp_array_t &al
 /* mp_gemm: W(A) and W(B), the signed residues scaled by 2^exp, go to ws
  * (gemm_workspace_bytes); with a smaller ws the chain runs step by step */
 size_t gemm_workspace_bytes(int nmod, int m, int n, int k);
+/* the split form's scratch (32 moduli; 0 for the other sets, which do not take
+ * that form): W(A), W(B), the modular product and the scalar chain's results,
+ * about (mk + kn + mn) * 4n + 48 mn bytes.  A ws of at least this size selects it. */
+size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k);
 cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
                         const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
                         Workspace ws, cudaStream_t s);
