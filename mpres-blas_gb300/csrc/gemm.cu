@@ -195,9 +195,75 @@ __device__ __forceinline__ er32 er_md32(const er32 &x, const er32 &y, const er_t
     return r;
 }
 
+/* er_md32 with the significands' product from one directed FP64
+ * multiplication -- what er_md's own __dmul_rd / __dmul_ru computes, correctly
+ * rounded, so the same 53 bits and exponent as the integer form above -- and
+ * the division by the unit on the integer pipes as there.  For a kernel whose
+ * integer pipe is the busy one (the split form's scalar chain): one FP64
+ * instruction in place of the 106-bit product, its normalisation and rounding. */
+template <bool UP>
+__device__ __forceinline__ er32 er_md32_dp(const er32 &x, const er32 &y, const er_t &z, double zr, uint64_t zinv) {
+    constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
+    const uint64_t bx = dbits(x.frac), by = dbits(y.frac);
+    const uint32_t ex = (uint32_t)(bx >> 52) & 2047u, ey = (uint32_t)(by >> 52) & 2047u;
+    const uint64_t sgn = (bx ^ by) & kSign;
+    er32 r;
+    if (ex == 1023u && ey == 1023u) {
+        const bool up = UP != (sgn != 0);
+        /* x*y in [1, 4): the significand p and e = 52 + (exponent of the product) */
+        const uint64_t bp = dbits(dmul<UP>(x.frac, y.frac));
+        const uint64_t p = (bp & kMant) | kHidden;
+        const int e = (int)((bp >> 52) & 2047u) - 1023 + 52;
+        const uint64_t bz = dbits(z.frac);
+        const uint64_t mz = (bz & kMant) | kHidden;
+        const int ez = (int)((bz >> 52) & 2047) - 1023;
+        const bool k52 = p >= mz;
+        uint64_t thi, tlo;
+        mul_wide53x64(p, zinv, thi, tlo);
+        uint64_t q = k52 ? thi : ((thi << 1) | (tlo >> 63));
+        uint64_t rem = (k52 ? (p << 52) : (p << 53)) - q * mz;
+        if (rem >= mz) {
+            q++;
+            rem -= mz;
+        }
+        q += (up && rem) ? 1u : 0u;
+        int E = e - 52 - ez - (k52 ? 52 : 53);
+        if (q >> 53) {
+            q >>= 1;
+            E++;
+        }
+        r.exp = x.exp + y.exp - (int)z.exp + E + 52;
+        r.frac = bdbl(sgn | kBiasExpMask | (q & kMant));
+        return r;
+    }
+    if (((bx << 1) == 0 && ey != 2047u) || ((by << 1) == 0 && ex != 2047u)) {
+        r.exp = 0;
+        r.frac = bdbl(sgn);
+        return r;
+    }
+    r.exp = x.exp + y.exp - (int)z.exp;
+    r.frac = div_by_const<UP>(dmul<UP>(x.frac, y.frac), z.frac, zr);
+    er_adjust32(r);
+    return r;
+}
+
 template <int N> __device__ __forceinline__ bool needs_round32(const er32 &u) {
     const Tables<N> &t = T<N>();
     return dnz(u.frac) && u.exp >= t.mp_h && u.exp - t.mp_h + 1 > 0;
+}
+
+/* The high word of the sign bit, read from constant memory: a flip of a
+ * double's sign written with a literal mask may be compiled as a double
+ * negation, an instruction of the FP64 pipe; an XOR with an operand the
+ * compiler cannot know stays on the integer pipes.  Same bits either way. */
+__constant__ uint32_t kSignHiWord = 0x80000000u;
+__device__ __forceinline__ double dflip_i(double x) {
+    const uint64_t u = dbits(x);
+    return __hiloint2double((int)((uint32_t)(u >> 32) ^ kSignHiWord), (int)(uint32_t)u);
+}
+__device__ __forceinline__ double dscale_sign_i(double x, int f) {
+    if (f == 0) return bdbl(dbits(x) & kSign);
+    return f < 0 ? dflip_i(x) : x;
 }
 
 template <int N>
@@ -220,8 +286,8 @@ __device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_
     er32 ax[2], ay[2];
     ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
     ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
-    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
-    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
+    ax[0].frac = dscale_sign_i(x.ev[0].frac, fx); ax[1].frac = dscale_sign_i(x.ev[1].frac, fx);
+    ay[0].frac = dscale_sign_i(y.ev[0].frac, fy); ay[1].frac = dscale_sign_i(y.ev[1].frac, fy);
     er32 ev[2];
     ev[0] = er_add32<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
     ev[1] = er_add32<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
@@ -230,8 +296,8 @@ __device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_
     r.sign = sign;
     r.exp = (ex == 0) ? ey : ex;
     if (sign) {
-        r.ev[0].frac = dflip(ev[1].frac); r.ev[0].exp = ev[1].exp;
-        r.ev[1].frac = dflip(ev[0].frac); r.ev[1].exp = ev[0].exp;
+        r.ev[0].frac = dflip_i(ev[1].frac); r.ev[0].exp = ev[1].exp;
+        r.ev[1].frac = dflip_i(ev[0].frac); r.ev[1].exp = ev[0].exp;
     } else {
         r.ev[0] = ev[0];
         r.ev[1] = ev[1];
@@ -561,7 +627,7 @@ struct ChainOut {
 };
 
 template <int N, int BX, int BY>
-__global__ void __launch_bounds__(BX *BY, 6) gemm_scalar_chain(int m, int n, int k, SoA A, int lda, SoA B, int ldb,
+__global__ void __launch_bounds__(BX *BY, 8) gemm_scalar_chain(int m, int n, int k, SoA A, int lda, SoA B, int ldb,
                                                               ChainOut out) {
     extern __shared__ __align__(16) unsigned char chain_smem[];
     ScalTile<BX, BY> *tiles = reinterpret_cast<ScalTile<BX, BY> *>(chain_smem);
@@ -595,14 +661,28 @@ __global__ void __launch_bounds__(BX *BY, 6) gemm_scalar_chain(int m, int n, int
         const ScalTile<BX, BY> &tl = tiles[buf];
         const int k0 = tile * kKT1;
         const int kend = min(kKT1, k - k0);
+        /* The operands' exponents, checked once per tile by the whole block (the
+         * staged slots past m, n or k hold zeros): if one is outside the 32-bit
+         * form's range, every output of the block runs the per-output chain.
+         * Inside the range the sum's exponent needs no check of its own: a sum
+         * takes the exponent of one of its operands or their minimum, and the
+         * products' exponents ea + eb are within +-2^27. */
+        bool out_of_range = false;
+        for (int e = threadIdx.y * BX + tx; e < kKT1 * BX; e += BX * BY)
+            out_of_range |= !(fits32(tl.ae[e / BX][e % BX], kExp32 / 2) &&
+                              fits32(tl.aev[e / BX][0][e % BX].y, kExp32) &&
+                              fits32(tl.aev[e / BX][1][e % BX].y, kExp32));
+        for (int e = threadIdx.y * BX + tx; e < kKT1 * BY; e += BX * BY)
+            out_of_range |= !(fits32(tl.be[e / BY][e % BY], kExp32 / 2) &&
+                              fits32(tl.bev[e / BY][0][e % BY].y, kExp32) &&
+                              fits32(tl.bev[e / BY][1][e % BY].y, kExp32));
+        if (__syncthreads_or(out_of_range)) lazy = false;
         if (lazy) {
             for (int kk = 0; kk < kend; kk++) {
                 const longlong2 a0 = tl.aev[kk][0][tx], a1 = tl.aev[kk][1][tx];
                 const longlong2 b0 = tl.bev[kk][0][ty], b1 = tl.bev[kk][1][ty];
                 const int sa = tl.as[kk][tx], ea = tl.ae[kk][tx], sb = tl.bs[kk][ty], eb = tl.be[kk][ty];
-                if (!(fits32(ea, kExp32 / 2) && fits32(eb, kExp32 / 2) && fits32(a0.y, kExp32) &&
-                      fits32(a1.y, kExp32) && fits32(b0.y, kExp32) && fits32(b1.y, kExp32) &&
-                      fits32(s.exp, kExp32) && fits32(s.ev[0].exp, kExp32) && fits32(s.ev[1].exp, kExp32))) {
+                if (!(fits32(s.ev[0].exp, kExp32) && fits32(s.ev[1].exp, kExp32))) {
                     lazy = false;
                     break;
                 }
@@ -611,8 +691,8 @@ __global__ void __launch_bounds__(BX *BY, 6) gemm_scalar_chain(int m, int n, int
                 Scal32 p;
                 p.sign = sa ^ sb;
                 p.exp = ea + eb;
-                p.ev[0] = er_md32<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
-                p.ev[1] = er_md32<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                p.ev[0] = er_md32_dp<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                p.ev[1] = er_md32_dp<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
                 Scal32 r;
                 int nzx, nzy;
                 const bool decided = add_scalars32<N>(r, nzx, nzy, s, p);
@@ -683,6 +763,7 @@ __global__ void __launch_bounds__(256) gemm_prescale_kq(const int *digits, const
  * int4 [n][N/4][m]. */
 constexpr int kRT = 64, kCT = 32, kKT2 = 12;
 static_assert(kKT2 == 2 * kFoldEvery, "two folds per k tile");
+
 
 template <int N>
 __global__ void __launch_bounds__(256) gemm_residue_product(int m, int n, int k, const int4 *WA, const int4 *WB,
