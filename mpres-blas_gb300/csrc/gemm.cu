@@ -252,20 +252,6 @@ template <int N> __device__ __forceinline__ bool needs_round32(const er32 &u) {
     return dnz(u.frac) && u.exp >= t.mp_h && u.exp - t.mp_h + 1 > 0;
 }
 
-/* The high word of the sign bit, read from constant memory: a flip of a
- * double's sign written with a literal mask may be compiled as a double
- * negation, an instruction of the FP64 pipe; an XOR with an operand the
- * compiler cannot know stays on the integer pipes.  Same bits either way. */
-__constant__ uint32_t kSignHiWord = 0x80000000u;
-__device__ __forceinline__ double dflip_i(double x) {
-    const uint64_t u = dbits(x);
-    return __hiloint2double((int)((uint32_t)(u >> 32) ^ kSignHiWord), (int)(uint32_t)u);
-}
-__device__ __forceinline__ double dscale_sign_i(double x, int f) {
-    if (f == 0) return bdbl(dbits(x) & kSign);
-    return f < 0 ? dflip_i(x) : x;
-}
-
 template <int N>
 __device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_out, const Scal32 &x, const Scal32 &y) {
     const Tables<N> &t = T<N>();
@@ -286,8 +272,8 @@ __device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_
     er32 ax[2], ay[2];
     ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
     ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
-    ax[0].frac = dscale_sign_i(x.ev[0].frac, fx); ax[1].frac = dscale_sign_i(x.ev[1].frac, fx);
-    ay[0].frac = dscale_sign_i(y.ev[0].frac, fy); ay[1].frac = dscale_sign_i(y.ev[1].frac, fy);
+    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
+    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
     er32 ev[2];
     ev[0] = er_add32<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
     ev[1] = er_add32<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
@@ -296,8 +282,8 @@ __device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_
     r.sign = sign;
     r.exp = (ex == 0) ? ey : ex;
     if (sign) {
-        r.ev[0].frac = dflip_i(ev[1].frac); r.ev[0].exp = ev[1].exp;
-        r.ev[1].frac = dflip_i(ev[0].frac); r.ev[1].exp = ev[0].exp;
+        r.ev[0].frac = dflip(ev[1].frac); r.ev[0].exp = ev[1].exp;
+        r.ev[1].frac = dflip(ev[0].frac); r.ev[1].exp = ev[0].exp;
     } else {
         r.ev[0] = ev[0];
         r.ev[1] = ev[1];

@@ -60,13 +60,21 @@ __device__ __forceinline__ bool dnz(double d) { return (dbits(d) << 1) != 0; }
 __device__ __forceinline__ bool dneg(double d) { return (dbits(d) >> 63) && dnz(d); }
 /* x > 0 for a non-NaN double */
 __device__ __forceinline__ bool dpos(double d) { return !(dbits(d) >> 63) && dnz(d); }
+/* The high word of the sign bit, read from constant memory.  A flip of a
+ * double's sign written with a literal mask is compiled as a double negation,
+ * an instruction of the FP64 pipe (ncu counted 5 double additions a step in a
+ * loop whose code has 2); an XOR with an operand the compiler cannot know stays
+ * on the integer pipes.  Same bits either way. */
+static __constant__ uint32_t kSignHiWord = 0x80000000u;
 /* -x: the sign bit flipped (what IEEE negation does), on the integer pipes */
-__device__ __forceinline__ double dflip(double x) { return bdbl(dbits(x) ^ kSign); }
+__device__ __forceinline__ double dflip(double x) {
+    const uint64_t u = dbits(x);
+    return __hiloint2double((int)((uint32_t)(u >> 32) ^ kSignHiWord), (int)(uint32_t)u);
+}
 /* x * f for f in {-1, 0, 1}: exactly the IEEE product, computed on bits */
 __device__ __forceinline__ double dscale_sign(double x, int f) {
-    uint64_t u = dbits(x);
-    if (f == 0) return bdbl(u & kSign);
-    return f < 0 ? bdbl(u ^ kSign) : x;
+    if (f == 0) return bdbl(dbits(x) & kSign);
+    return f < 0 ? dflip(x) : x;
 }
 
 /* Conversions between integers and doubles on the integer pipes.  On GB300 a
