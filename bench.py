@@ -217,6 +217,43 @@ def probe_rates(torch, mp, stream):
     return out
 
 
+def gemm_roofline(torch, mp, stream, d, c_work, c_init, clocks, step_secs, rates, reps=3):
+    """Roofline of the dominant kernel of mp_gemm's split form, the scalar
+    chain: its launch timed live (mpres_probe_gemm_phases, events between the
+    six launches of one call, mean of `reps` calls on the same inputs), against
+    the SMs' instruction issue rate at the SM clock sampled during the timed
+    steps.  The kernel's work per launch is its warp instruction count for this
+    workload, from the committed ncu capture (profiles/ncu_traffic.json): the
+    kernel is bound by its integer pipe, and its interval arithmetic has no
+    HBM or tensor bound."""
+    m, n = 1024, 32
+    phases = None
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            c_work.copy_(c_init)
+        ph = mp.probe_gemm_phases(n, m, m, m, d["alpha"], d["A"], m, d["B"], m, d["beta"], c_work, m, stream=stream)
+        phases = ph if phases is None else {k: phases[k] + ph[k] for k in ph}
+    phases = {k: v / reps for k, v in phases.items()}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or 2070.0
+    peak = 4.0 * sms * mhz * 1e6  # warp instructions issued per second: four schedulers an SM
+    entry = json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())["kernels"].get("gemm_scalar_chain", {}) \
+        if (ROOT / "profiles" / "ncu_traffic.json").exists() else {}
+    inst = entry.get("warp_instructions_per_launch")
+    t = phases["scalar_chain"] / 1e3
+    achieved = inst / t if inst else None
+    return {"bound": "int", "kernel": "gemm_scalar_chain", "achieved": achieved / 1e9 if achieved else None,
+            "peak": peak / 1e9, "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
+            "traffic": entry.get("bytes_per_launch"), "kernel_ms": phases["scalar_chain"],
+            "share_of_step": t / step_secs, "phases_ms": phases,
+            "alu_pipe_active": entry.get("alu_pipe_active"),
+            "peak_source": "4 warp instructions per cycle per SM x %d SMs x the sampled SM clock" % sms,
+            "work_note": "a split-form step: W(A), W(B); the scalar chain (sign, exponent and interval of every "
+                         "k step, the reference's expressions); the residues as one modular product W(A) x W(B) "
+                         "per modulus (%.2f G 64-bit multiply-adds); the epilogue" % (n * m ** 3 / 1e9),
+            "mulmod_peak_G": rates["mulmod"] / 1e9, "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
+
+
 def gemm_config(world):
     """The headline workload, named identically by both arms."""
     return {"workload": "mp_gemm m=n=k=1024, 32 moduli (params.32_32bit), NN, column-major", "global_batch": 1,
@@ -276,16 +313,7 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     value = world * ops * steps / secs
     resident_c = c_work.download()
     rates = probe_rates(torch, mp, stream)
-    w_int = 3.0 * m * m * m * n  # Barrett products per launch (1 in the multiply, 2 in the aligned add)
-    per_launch = secs / steps
-    achieved = w_int / per_launch
-    roof = {"bound": "int", "achieved": achieved / 1e9, "peak": rates["mulmod"] / 1e9, "unit": "Gmulmod/s",
-            "frac": achieved / rates["mulmod"], "traffic": traffic("gemm_nn_tiled"),
-            "peak_source": "measured in this run: Barrett mulmod microkernel (probe.cu)",
-            "work_note": "achieved counts the reference chain's 3*m*n*k*N modular products; the lazy-residue "
-                         "chain forms one 64-bit multiply-add per residue and step instead, and the interval "
-                         "arithmetic of each step binds",
-            "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
+    roof = gemm_roofline(torch, mp, stream, d, c_work, c_init, clk.summary(), secs / steps, rates)
 
     # e2e: host mp_float_t arrays in pinned memory through the C ABI copies,
     # every step: upload A, B, C; mp_gemm into C; download the product
@@ -305,9 +333,10 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     e2e = {"value": world * ops * steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": 3 * m * m * sz,
            "d2h_bytes_per_step": m * m * sz, "steps": steps,
            "result_matches_resident": bool(c_out.tobytes() == resident_c.tobytes())}
-    # per step: gemm_prescale for A and for B, then gemm_nn_lazy (the restore of C is a torch copy)
+    # per step: gemm_prescale for A and for B, the scalar chain, the modular product, the epilogue and the
+    # per-output chain of the outputs that leave the split form (the restore of C is a torch copy)
     return dict(secs=secs, value=value, roofline=roof, e2e=e2e, clocks=clk.summary(), host=host, src=src,
-                launches=3 * steps)
+                launches=6 * steps)
 
 
 def chain_cycles(mp, n, kind, x, y, length):

@@ -804,6 +804,27 @@ int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long c
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_fraction_sum");
 }
 
+int mpres_probe_gemm_phases(int nmod, int m, int n, int k, const mp_array_t *alpha, const mp_array_t *A, int lda,
+                            const mp_array_t *B, int ldb, const mp_array_t *beta, mp_array_t *C, int ldc, float *ms,
+                            void *stream) {
+    if (int st = require(nmod)) return st;
+    if (!alpha || !A || !B || !beta || !C || !ms || m <= 0 || n <= 0 || k <= 0 || lda < m || ldb < k || ldc < m)
+        return fail(MPRES_ERR_INVALID_VALUE, "mpres_probe_gemm_phases: bad arguments");
+    if (nmod != 32) return fail(MPRES_ERR_NOT_SUPPORTED, "mpres_probe_gemm_phases: the split form is for 32 moduli");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Workspace ws;
+    if (int st = workspace(s, gemm_split_workspace_bytes(nmod, m, n, k), ws)) return st;
+    cudaEvent_t ev[7] = {};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 7 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
+    if (e == cudaSuccess) e = launch_gemm_split_marked(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s, ev);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[6]);
+    for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    for (int i = 0; i < 7; i++)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_gemm_phases");
+}
+
 int mpres_probe_eval_phases(int nmod, const int *digits, int count, long long *cycles, int *out, void *stream) {
     if (int st = require(nmod)) return st;
     if (count <= 0 || !digits || !cycles || !out)

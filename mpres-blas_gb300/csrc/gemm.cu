@@ -249,7 +249,7 @@ __device__ __forceinline__ er32 er_md32_dp(const er32 &x, const er32 &y, const e
 
 template <int N> __device__ __forceinline__ bool needs_round32(const er32 &u) {
     const Tables<N> &t = T<N>();
-    return dnz(u.frac) && u.exp >= t.mp_h && u.exp - t.mp_h + 1 > 0;
+    return dnz(u.frac) && u.exp >= t.mp_h; /* then u.exp - mp_h + 1 > 0 as well */
 }
 
 template <int N>
@@ -867,6 +867,11 @@ __global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alp
     s.ev[0] = in.ev[e];
     s.ev[1] = in.ev[mn + e];
     const int4 *ws = WS + (size_t)col * Q * m + row;
+    /* D = W * 2^-e: 2^-e from the RNS_POW2 row -e when 0 <= -e <= log2m (a sum's
+     * exponent is its smallest product's, so usually), else by squaring */
+    const long long ne = -(long long)s.exp;
+    const bool row_ok = ne >= 0 && ne <= t.log2m;
+    const int *p2 = t.pow2 + (size_t)(row_ok ? ne : 0) * N;
 #pragma unroll
     for (int q = 0; q < Q; q++) {
         const int4 v = __ldg(ws + (size_t)q * m);
@@ -875,7 +880,8 @@ __global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alp
         for (int j = 0; j < 4; j++) {
             const int i = 4 * q + j;
             const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
-            const uint32_t d = mulmod(vv[j], pow2mod(-(long long)s.exp, md, mu), md, mu);
+            const uint32_t f = row_ok ? (uint32_t)__ldg(p2 + i) : pow2mod(ne, md, mu);
+            const uint32_t d = mulmod(vv[j], f, md, mu);
             s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
         }
     }
@@ -939,10 +945,12 @@ size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp
     return off;
 }
 
+/* marks: null, or seven events recorded on s before the first launch and
+ * after each of the six launches (the phases' times for the probe) */
 template <int N>
 cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
                       const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
-                      Workspace ws, cudaStream_t s) {
+                      Workspace ws, cudaStream_t s, cudaEvent_t *marks = nullptr) {
     constexpr int BX = 32, BY = 4;
     SplitScratch sp;
     split_scratch(N, m, n, k, ws.ptr, &sp);
@@ -968,18 +976,26 @@ cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_arr
     });
     if (rgrid <= 0) return cudaErrorInvalidDevice;
     if ((e = cudaMemsetAsync(sp.out.nredo, 0, sizeof(int), s)) != cudaSuccess) return e;
+    auto mark = [&](int i) { if (marks) cudaEventRecord(marks[i], s); };
+    mark(0);
     gemm_prescale<N, true><<<(unsigned)((na + 255) / 256), 256, 0, s>>>(A.digits, A.sign, A.exp, lda, m, k, sp.wa);
+    mark(1);
     gemm_prescale_kq<N><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, sp.wb);
+    mark(2);
     gemm_scalar_chain<N, BX, BY><<<(unsigned)(gx * gy), dim3(BX, BY), smem, s>>>(m, n, k, soa(A), lda, soa(B), ldb,
                                                                               sp.out);
+    mark(3);
     gemm_residue_product<N><<<dim3((unsigned)(rt * ct), N / 4), 256, 0, s>>>(m, n, k, sp.wa, sp.wb, sp.ws);
+    mark(4);
     er_t *cv = reinterpret_cast<er_t *>(C.eval);
     gemm_split_epilogue<N><<<(unsigned)((mn + 127) / 128), 128, 0, s>>>(m, n, soa(alpha), soa(beta), C.digits, C.sign,
                                                                          C.exp, cv, C.len, ldc, sp.ws, sp.out);
+    mark(5);
     const long long want = (mn + 127) / 128;
     gemm_redo<N><<<(unsigned)(want < rgrid ? want : rgrid), 128, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B),
                                                                          ldb, soa(beta), C.digits, C.sign, C.exp, cv,
                                                                          C.len, ldc, sp.wa, sp.wb, sp.out);
+    mark(6);
     return cudaGetLastError();
 }
 
@@ -1028,6 +1044,14 @@ size_t gemm_workspace_bytes(int nmod, int m, int n, int k) {
 size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k) {
     if (nmod != 32) return 0;
     return split_scratch(nmod, m, n, k, nullptr, nullptr);
+}
+
+cudaError_t launch_gemm_split_marked(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A,
+                                     int lda, const mp_array_t &B, int ldb, const mp_array_t &beta,
+                                     const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s, cudaEvent_t *marks) {
+    if (nmod != 32 || ws.ptr == nullptr || ws.bytes < gemm_split_workspace_bytes(nmod, m, n, k))
+        return cudaErrorNotSupported;
+    return run_split<32>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s, marks);
 }
 
 cudaError_t launch_gemm(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,

@@ -112,6 +112,7 @@ _SIGS = {
     "mpres_probe_chain": (I, [I, I, P, P, I, P, P, P, P]),
     "mpres_probe_rounding": (I, [I, P, P, I, P, P, P]),
     "mpres_probe_eval_phases": (I, [I, P, I, P, P, P]),
+    "mpres_probe_gemm_phases": (I, [I, I, I, I, P, P, I, P, I, P, P, I, P, P]),
     "mpres_probe_fraction_sum": (I, [I, I, P, ctypes.c_longlong, P, P, P]),
     "mpres_rns_scale2pow": (I, [I, P, P, P, SZ, P]),
     "mpres_rns_eval": (I, [I, I, P, P, P, SZ, P]),
@@ -525,6 +526,18 @@ def gemm(nmod, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, transa=NO_TRANS, tr
     b1x, b1y, g2x, g2y, b3 = order
     check(lib().mpres_gemm(nmod, transa, transb, m, n, k, alpha.ref, A.ref, lda, B.ref, ldb, beta.ref, C.ref, ldc,
                            None, b1x, b1y, g2x, g2y, b3, _stream_handle(stream)), "mpres_gemm")
+
+
+GEMM_PHASES = ("prescale_a", "prescale_b", "scalar_chain", "residue_product", "epilogue", "redo")
+
+
+def probe_gemm_phases(nmod, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream=None):
+    """mp_gemm's split form (32 moduli) with each of its six launches timed by
+    events (mpres_probe_gemm_phases): {phase: milliseconds}, GEMM_PHASES order."""
+    ms = (ctypes.c_float * 6)()
+    check(lib().mpres_probe_gemm_phases(nmod, m, n, k, alpha.ref, A.ref, lda, B.ref, ldb, beta.ref, C.ref, ldc, ms,
+                                        _stream_handle(stream)), "mpres_probe_gemm_phases")
+    return dict(zip(GEMM_PHASES, list(ms)))
 
 
 def spmv_csr(nmod, m, csr, x, y, threads=32, stream=None):

@@ -253,6 +253,25 @@ def test_gemm_without_scratch_vs_oracle(gpu, oracle, monkeypatch, n, lo, hi):
     eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
 
 
+def test_gemm_phase_probe_matches_gemm(gpu, oracle):
+    """mpres_probe_gemm_phases runs mp_gemm's split form (32 moduli) with an
+    event between its launches: the oracle's bits, and a time for each launch."""
+    n, m, cols, k = 32, 70, 45, 90
+    rng = np.random.default_rng(helpers.SEED + 23)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, -32, 32))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, -32, 32))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    dA, dB, dC = (gpu.DeviceArray.from_host(n, v) for v in (A, B, C))
+    da, db = gpu.DeviceArray.from_host(n, al), gpu.DeviceArray.from_host(n, be)
+    ms = gpu.probe_gemm_phases(n, m, cols, k, da, dA, m, dB, k, db, dC, m)
+    sync()
+    eq(dC.download(), oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m))
+    assert list(ms) == list(gpu.GEMM_PHASES) and all(v > 0 for v in ms.values())
+    with pytest.raises(gpu.MpresError):
+        gpu.probe_gemm_phases(8, 2, 2, 2, da, dA, 2, dB, 2, db, dC, 2)
+
+
 def test_gemm_transposed_is_not_supported(gpu):
     rec = gpu.set_d(8, np.ones(4))
     d = gpu.DeviceArray.from_host(8, rec)
