@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(256) gemm_prescale(const int *digits, const in
 
 /* ------------- the scalar half of a step with 32-bit exponents --------------
  *
- * The same expressions as er_md / er_add / add_scalars / needs_round with the
+ * The same values as er_md / er_add / add_scalars / needs_round with the
  * exponents held in 32-bit integers: identical values as long as nothing
  * overflows, which the callers guarantee by taking this form only when every
  * exponent entering the step is within +-2^27 (the operands' exponents within
@@ -142,65 +142,13 @@ template <bool UP> __device__ __forceinline__ er32 er_add32(const er32 &x, const
     return r;
 }
 
-template <bool UP>
-__device__ __forceinline__ er32 er_md32(const er32 &x, const er32 &y, const er_t &z, double zr, uint64_t zinv) {
-    constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
-    const uint64_t bx = dbits(x.frac), by = dbits(y.frac);
-    const uint32_t ex = (uint32_t)(bx >> 52) & 2047u, ey = (uint32_t)(by >> 52) & 2047u;
-    const uint64_t sgn = (bx ^ by) & kSign;
-    er32 r;
-    if (ex == 1023u && ey == 1023u) {
-        const bool up = UP != (sgn != 0);
-        const uint64_t mx = (bx & kMant) | kHidden, my = (by & kMant) | kHidden;
-        uint64_t hi, lo;
-        mul_wide53(mx, my, hi, lo);
-        const int sh = (hi >> 41) ? 53 : 52;
-        uint64_t p = (hi << (64 - sh)) | (lo >> sh);
-        p += (up && (lo & ((1ull << sh) - 1))) ? 1u : 0u;
-        int e = sh;
-        if (p >> 53) {
-            p >>= 1;
-            e++;
-        }
-        const uint64_t bz = dbits(z.frac);
-        const uint64_t mz = (bz & kMant) | kHidden;
-        const int ez = (int)((bz >> 52) & 2047) - 1023;
-        const bool k52 = p >= mz;
-        uint64_t thi, tlo;
-        mul_wide53x64(p, zinv, thi, tlo);
-        uint64_t q = k52 ? thi : ((thi << 1) | (tlo >> 63));
-        uint64_t rem = (k52 ? (p << 52) : (p << 53)) - q * mz;
-        if (rem >= mz) {
-            q++;
-            rem -= mz;
-        }
-        q += (up && rem) ? 1u : 0u;
-        int E = e - 52 - ez - (k52 ? 52 : 53);
-        if (q >> 53) {
-            q >>= 1;
-            E++;
-        }
-        r.exp = x.exp + y.exp - (int)z.exp + E + 52;
-        r.frac = bdbl(sgn | kBiasExpMask | (q & kMant));
-        return r;
-    }
-    if (((bx << 1) == 0 && ey != 2047u) || ((by << 1) == 0 && ex != 2047u)) {
-        r.exp = 0;
-        r.frac = bdbl(sgn);
-        return r;
-    }
-    r.exp = x.exp + y.exp - (int)z.exp;
-    r.frac = div_by_const<UP>(dmul<UP>(x.frac, y.frac), z.frac, zr);
-    er_adjust32(r);
-    return r;
-}
-
-/* er_md32 with the significands' product from one directed FP64
- * multiplication -- what er_md's own __dmul_rd / __dmul_ru computes, correctly
- * rounded, so the same 53 bits and exponent as the integer form above -- and
- * the division by the unit on the integer pipes as there.  For a kernel whose
- * integer pipe is the busy one (the split form's scalar chain): one FP64
- * instruction in place of the 106-bit product, its normalisation and rounding. */
+/* er_md (mp_device.cuh) in the 32-bit exponent form, with the significands'
+ * product from one directed FP64 multiplication (er_md's DP form: what
+ * __dmul_rd / __dmul_ru compute, correctly rounded, so the same 53 bits and
+ * exponent as the integer product) and the division by the unit on the integer
+ * pipes.  The GEMM chains are bound by their integer pipe: one FP64 instruction
+ * in place of the 106-bit product, its normalisation and rounding (the split
+ * form's scalar chain, 1024^3: 19.1 -> 16.0 ms). */
 template <bool UP>
 __device__ __forceinline__ er32 er_md32_dp(const er32 &x, const er32 &y, const er_t &z, double zr, uint64_t zinv) {
     constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
@@ -464,8 +412,8 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_tiled(int m, int n, int k, 
                         Scal32 p;
                         p.sign = sa ^ sb;
                         p.exp = ea + eb;
-                        p.ev[0] = er_md32<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
-                        p.ev[1] = er_md32<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                        p.ev[0] = er_md32_dp<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                        p.ev[1] = er_md32_dp<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
                         Scal32 r;
                         int nzx, nzy;
                         const bool decided = add_scalars32<N>(r, nzx, nzy, s32, p);

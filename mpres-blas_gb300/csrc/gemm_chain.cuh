@@ -290,8 +290,8 @@ __device__ __forceinline__ void gemm_lazy_output(int m, int k, const MatSoA &alp
                 Scal p;
                 p.sign = sa ^ sb;
                 p.exp = ea + eb;
-                p.ev[0] = er_md<false>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
-                p.ev[1] = er_md<true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
+                p.ev[0] = er_md<false, true>(ae0, be0, t.unit_upp, t.unit_upp_recip, t.unit_upp_inv);
+                p.ev[1] = er_md<true, true>(ae1, be1, t.unit_low, t.unit_low_recip, t.unit_low_inv);
                 Scal r;
                 int nzx, nzy;
                 const bool decided = add_scalars<N>(r, nzx, nzy, sum, p);
