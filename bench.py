@@ -220,7 +220,7 @@ def probe_rates(torch, mp, stream):
 def gemm_roofline(torch, mp, stream, d, c_work, c_init, clocks, step_secs, rates, reps=3):
     """Roofline of the dominant kernel of mp_gemm's split form, the scalar
     chain: its launch timed live (mpres_probe_gemm_phases, events between the
-    six launches of one call, mean of `reps` calls on the same inputs), against
+    launches of one call, mean of `reps` calls on the same inputs), against
     the SMs' instruction issue rate at the SM clock sampled during the timed
     steps.  The kernel's work per launch is its warp instruction count for this
     workload, from the committed ncu capture (profiles/ncu_traffic.json): the
@@ -248,9 +248,10 @@ def gemm_roofline(torch, mp, stream, d, c_work, c_init, clocks, step_secs, rates
             "share_of_step": t / step_secs, "phases_ms": phases,
             "alu_pipe_active": entry.get("alu_pipe_active"),
             "peak_source": "4 warp instructions per cycle per SM x %d SMs x the sampled SM clock" % sms,
-            "work_note": "a split-form step: W(A), W(B); the scalar chain (sign, exponent and interval of every "
-                         "k step, the reference's expressions); the residues as one modular product W(A) x W(B) "
-                         "per modulus (%.2f G 64-bit multiply-adds); the epilogue" % (n * m ** 3 / 1e9),
+            "work_note": "a split-form step: W(A), W(B) and their bf16 limb planes; the scalar chain (sign, "
+                         "exponent and interval of every k step, the reference's expressions); the residues as one "
+                         "modular product W(A) x W(B) per modulus on the tensor cores (16 limb products, %.2f TFLOP "
+                         "of bf16 mma.sync); the epilogue" % (16 * n * 2 * m ** 3 / 1e12),
             "mulmod_peak_G": rates["mulmod"] / 1e9, "fp64_dadd_rd_peak_G": rates["dadd_rd"] / 1e9}
 
 
@@ -333,10 +334,10 @@ def bench_gemm(torch, mp, stream, steps, warmup, world, rank, local):
     e2e = {"value": world * ops * steps / e2e_secs, "unit": "MP ops/s", "h2d_bytes_per_step": 3 * m * m * sz,
            "d2h_bytes_per_step": m * m * sz, "steps": steps,
            "result_matches_resident": bool(c_out.tobytes() == resident_c.tobytes())}
-    # per step: gemm_prescale for A and for B, the scalar chain, the modular product, the epilogue and the
-    # per-output chain of the outputs that leave the split form (the restore of C is a torch copy)
+    # per step: gemm_prescale for A and for B, the limb planes of each, the scalar chain, the modular product, the
+    # epilogue and the per-output chain of the outputs that leave the split form (the restore of C is a torch copy)
     return dict(secs=secs, value=value, roofline=roof, e2e=e2e, clocks=clk.summary(), host=host, src=src,
-                launches=6 * steps)
+                launches=8 * steps)
 
 
 def chain_cycles(mp, n, kind, x, y, length):

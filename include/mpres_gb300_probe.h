@@ -87,11 +87,12 @@ int mpres_probe_fraction_sum(int nmod, int which, const int *digits, long long c
  * sum}; out = int[32] checksum.  Device memory. */
 int mpres_probe_eval_phases(int nmod, const int *digits, int count, long long *cycles, int *out, void *stream);
 
-/* mp_gemm (no transposes, 32 moduli) in its split form -- W(A), W(B), the scalar
- * chain, the modular product, the epilogue, the per-output chain of the outputs
- * that leave that form -- with an event between every two of its six launches:
- * ms = float[6] receives each launch's time, after the call has completed on
- * `stream`.  Same arguments and results as mpres_gemm otherwise. */
+/* mp_gemm (no transposes, 32 moduli) in its split form with an event between
+ * its phases: ms = float[7] receives the time of each -- W(A), W(B), their limb
+ * planes, the scalar chain, the modular product on the tensor cores, the
+ * epilogue, the per-output chain of the outputs that leave that form -- after
+ * the call has completed on `stream`.  Same arguments and results as mpres_gemm
+ * otherwise. */
 int mpres_probe_gemm_phases(int nmod, int m, int n, int k, const mp_array_t *alpha, const mp_array_t *A, int lda,
                             const mp_array_t *B, int ldb, const mp_array_t *beta, mp_array_t *C, int ldc, float *ms,
                             void *stream);

@@ -814,13 +814,14 @@ int mpres_probe_gemm_phases(int nmod, int m, int n, int k, const mp_array_t *alp
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Workspace ws;
     if (int st = workspace(s, gemm_split_workspace_bytes(nmod, m, n, k), ws)) return st;
-    cudaEvent_t ev[7] = {};
+    constexpr int P = kGemmSplitPhases;
+    cudaEvent_t ev[P + 1] = {};
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < 7 && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
+    for (int i = 0; i <= P && e == cudaSuccess; i++) e = cudaEventCreate(&ev[i]);
     if (e == cudaSuccess) e = launch_gemm_split_marked(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s, ev);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[6]);
-    for (int i = 0; i < 6 && e == cudaSuccess; i++) e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
-    for (int i = 0; i < 7; i++)
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[P]);
+    for (int i = 0; i < P && e == cudaSuccess; i++) e = cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    for (int i = 0; i <= P; i++)
         if (ev[i]) cudaEventDestroy(ev[i]);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_probe_gemm_phases");
 }

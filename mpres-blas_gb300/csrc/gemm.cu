@@ -502,9 +502,10 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_tiled(int m, int n, int k, 
  *   gemm_scalar_chain   the scalar chain of every output (sign, exponent,
  *                       interval), no residues: no 64-bit accumulators live in
  *                       the loop, so more warps share an SM;
- *   gemm_residue_product  W(A) x W(B) per modulus quad, tiled through shared
- *                       memory, 64-bit lazy accumulators folded every six
- *                       steps;
+ *   gemm_limbs, gemm_mma_product  W(A) x W(B) per modulus on the tensor
+ *                       cores: each residue as four 8-bit limbs in bf16, the
+ *                       limb products summed exactly in fp32 and weighted by
+ *                       2^(8s) mod m_j in 64-bit integers;
  *   gemm_split_epilogue the residues of each sum recovered as
  *                       (-1)^s * W * 2^-e, then alpha*sum, beta*C and the split
  *                       addition as in the other kernels;
@@ -513,7 +514,8 @@ __global__ void __launch_bounds__(BX *BY, 3) gemm_nn_tiled(int m, int n, int k, 
  *                       exponents outside the 32-bit range) run the
  *                       per-output lazy chain from the start instead.
  * Every value is the one the single chain computes, so results are the same
- * bits.  The scratch grows by about the size of C (4N + 48 bytes an output). */
+ * bits.  The scratch: W(A), W(B), their limb planes (twice the size of W), the
+ * product (the size of C's residues) and 48 bytes an output. */
 constexpr int kKT1 = 8;   /* k steps per staged tile of the scalar chain */
 constexpr int kRedo = 2;  /* sign marker: the output runs the per-output chain */
 
@@ -688,111 +690,175 @@ __global__ void __launch_bounds__(256) gemm_prescale_kq(const int *digits, const
     }
 }
 
-/* S = W(A) x W(B) mod m_j for the four moduli of quad blockIdx.y: a block
- * computes a kRT x kCT tile of S, lane l of warp w the rows l and l + 32 and
- * the columns 4w .. 4w + 3 (32 accumulators of 64 bits); the k tiles of W(A)
- * (kRT int4 a step) and W(B) (kCT int4) are staged by cp.async, double
- * buffered.  A product is below m^2 < 2^60.6 and a folded accumulator below
- * 2^62.3, so six products go between folds.  The result, reduced, goes to
- * int4 [n][N/4][m]. */
-constexpr int kRT = 64, kCT = 32, kKT2 = 12;
-static_assert(kKT2 == 2 * kFoldEvery, "two folds per k tile");
+/* ---------------- the modular product on the tensor cores -------------------
+ *
+ * S_j = W_j(A) x W_j(B) mod m_j for every modulus j.  A residue w < m_j < 2^30.3
+ * is the sum of four limbs w = l0 + l1 2^8 + l2 2^16 + l3 2^24 (l0..l2 <= 255,
+ * l3 <= 78), each exact in bf16, so S_j = sum_s 2^(8s) G_s with
+ * G_s = sum_{a+b=s} L_a(A) x L_b(B), seven limb-sum groups of sixteen bf16 products.
+ * The tensor cores sum a group over one stage of kKC = 32 k steps in fp32,
+ * started at 2^23: every partial sum is an integer below 2^24 (the largest group,
+ * s = 2, is at most 3 x 32 x 255^2 < 6.3e6 < 2^23), so the additions are exact and
+ * the group's value is the significand of the result (integer sums that large
+ * measured exact on this GPU with the same mma.sync form).  Each group's value
+ * then enters a 64-bit accumulator times 2^(8s) mod m_j: below 2^23 * 2^30.3 per
+ * term, seven terms a stage, folded (2^32 mod m_j) every kFoldStages stages.  Same
+ * residues as the integer product, bit for bit. */
+constexpr int kTB = 64;         /* outputs per block side */
+constexpr int kKC = 32;         /* k steps per stage and per fp32 group sum */
+constexpr int kFoldStages = 128; /* 896 terms below 2^53.3 on a folded value below 2^62.3 stay below 2^64 */
 
-
-template <int N>
-__global__ void __launch_bounds__(256) gemm_residue_product(int m, int n, int k, const int4 *WA, const int4 *WB,
-                                                           int4 *WS) {
-    constexpr int Q = N / 4;
-    __shared__ __align__(16) int4 sa[2][kKT2][kRT];
-    __shared__ __align__(16) int4 sb[2][kKT2][kCT];
-    const Tables<N> &t = T<N>();
-    const int q = blockIdx.y;
-    const int gx = (m + kRT - 1) / kRT;
-    const int r0 = (blockIdx.x % gx) * kRT, c0 = (blockIdx.x / gx) * kCT;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    uint32_t c32[4], mods[4], mus[4];
+/* W (int4 [k][8][rows], 32 moduli) as limb planes bf16 [32][4][kp][rows_p], rows_p
+ * and kp the padded sizes (multiples of kTB and kKC), zeros in the padding */
+__global__ void __launch_bounds__(256) gemm_limbs(const int4 *W, int rows, int k, int rows_p, int kp, uint16_t *L) {
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; /* e = kk * rows_p + r */
+    if (e >= (long long)rows_p * kp) return;
+    const int r = (int)(e % rows_p), kk = (int)(e / rows_p);
+    const bool in = r < rows && kk < k;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-        c32[j] = t.pow2_32[4 * q + j];
-        mods[j] = (uint32_t)t.moduli[4 * q + j];
-        mus[j] = t.mu[4 * q + j];
+    for (int q = 0; q < 8; q++) {
+        const int4 w = in ? __ldg(W + ((size_t)kk * 8 + q) * rows + r) : make_int4(0, 0, 0, 0);
+        const uint32_t v[4] = {(uint32_t)w.x, (uint32_t)w.y, (uint32_t)w.z, (uint32_t)w.w};
+#pragma unroll
+        for (int x = 0; x < 4; x++)
+#pragma unroll
+            for (int a = 0; a < 4; a++) /* an integer below 256 as bf16: the top half of its float */
+                L[(((size_t)(4 * q + x) * 4 + a) * kp + kk) * rows_p + r] =
+                    (uint16_t)(__float_as_uint((float)((v[x] >> (8 * a)) & 255u)) >> 16);
     }
-    uint64_t acc[2][4][4];
+}
+
+__device__ __forceinline__ void ldsm4t(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+__device__ __forceinline__ void mma_bf16(float *d, const uint32_t *a, uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+                 "{%0, %1, %2, %3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+__device__ __forceinline__ void cp_async16_cg(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+
+/* A block: a kTB x kTB tile of S_j, j = blockIdx.y; four warps of 32 x 32 (2 x 4
+ * tiles of 16 x 8).  Per stage the four limb planes of A and of B (kKC rows of
+ * kTB bf16, 128 bytes, 16-byte chunks XOR-swizzled by row so that ldmatrix reads
+ * are free of bank conflicts) come in by cp.async, double buffered (64 KB); a
+ * warp keeps the stage's A fragments (all limbs, both k16 steps) in registers
+ * and loads B fragments per limb pair.  Output: u32 [32][n][m]. */
+__global__ void __launch_bounds__(128, 2) gemm_mma_product(int m, int n, int mp, int np, int kp, const uint16_t *LA,
+                                                           const uint16_t *LB, uint32_t *S) {
+    extern __shared__ __align__(128) unsigned char prod_smem[];
+    const Tables<32> &t = T<32>();
+    const int j = blockIdx.y, gx = mp / kTB;
+    const int r0 = (blockIdx.x % gx) * kTB, c0 = (blockIdx.x / gx) * kTB;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int wm = (w & 1) * 32, wn = (w >> 1) * 32;
+    const uint32_t md = (uint32_t)t.moduli[j], mu = t.mu[j], c32 = t.pow2_32[j];
+    uint32_t wt[7]; /* 2^(8s) mod m_j */
+    wt[0] = 1u;
 #pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int x = 0; x < 4; x++) acc[i][j][x] = 0;
-    auto stage = [&](int buf, int k0) {
-        for (int e = threadIdx.x; e < kKT2 * kRT; e += 256) {
-            const int kk = e / kRT, r = e % kRT;
-            const bool ok = (k0 + kk < k) && (r0 + r < m);
-            const int4 *src = ok ? WA + ((size_t)(k0 + kk) * Q + q) * m + r0 + r : WA;
-            cp_async16((uint32_t)__cvta_generic_to_shared(&sa[buf][kk][r]), src, ok);
-        }
-        for (int e = threadIdx.x; e < kKT2 * kCT; e += 256) {
-            const int kk = e / kCT, c = e % kCT;
-            const bool ok = (k0 + kk < k) && (c0 + c < n);
-            const int4 *src = ok ? WB + ((size_t)(k0 + kk) * Q + q) * n + c0 + c : WB;
-            cp_async16((uint32_t)__cvta_generic_to_shared(&sb[buf][kk][c]), src, ok);
+    for (int s = 1; s < 7; s++) wt[s] = mulmod(wt[s - 1], 256u, md, mu);
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(prod_smem);
+    auto stage = [&](int st, int k0) {
+        /* 2 operands x 4 limbs x kKC rows x 8 chunks of 16 bytes */
+        for (int e = tid; e < 2 * 4 * kKC * 8; e += 128) {
+            const int op = e >> 10, a = (e >> 8) & 3, kk = (e >> 3) & 31, c = e & 7;
+            const uint16_t *src = op == 0 ? LA + (((size_t)(j * 4 + a) * kp + k0 + kk) * mp + r0 + 8 * c)
+                                          : LB + (((size_t)(j * 4 + a) * kp + k0 + kk) * np + c0 + 8 * c);
+            cp_async16_cg(sbase + st * 32768 + op * 16384 + (a * kKC + kk) * 128 + ((c ^ (kk & 7)) << 4), src);
         }
     };
-    const int ntiles = (k + kKT2 - 1) / kKT2;
+    static_assert(kKC == 32 && kTB == 64, "the staging index arithmetic assumes these sizes");
+    uint64_t acc[2][4][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) acc[mt][nt][i] = 0;
+    const int nst = kp / kKC;
+    const int mi = lane >> 3, r8 = lane & 7;
     stage(0, 0);
     cp_async_commit();
-    for (int tile = 0; tile < ntiles; tile++) {
-        const int buf = tile & 1;
-        if (tile + 1 < ntiles) stage(buf ^ 1, (tile + 1) * kKT2);
+    for (int st = 0; st < nst; st++) {
+        if (st + 1 < nst) stage((st + 1) & 1, (st + 1) * kKC);
         cp_async_commit();
         cp_async_wait_one();
         __syncthreads();
+        const uint32_t sA = sbase + (st & 1) * 32768, sB = sA + 16384;
+        uint32_t af[2][4][2][4]; /* [k16 step][limb][m16 tile][register] */
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
-            /* staged zeros past k add nothing, so every tile runs its full length */
+        for (int ks = 0; ks < 2; ks++)
 #pragma unroll
-            for (int kk = h * kFoldEvery; kk < (h + 1) * kFoldEvery; kk++) {
-                const int4 a0 = sa[buf][kk][lane], a1 = sa[buf][kk][lane + 32];
+            for (int a = 0; a < 4; a++)
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const int4 b = sb[buf][kk][4 * w + j];
-                    acc[0][j][0] += (uint64_t)(uint32_t)a0.x * (uint32_t)b.x;
-                    acc[0][j][1] += (uint64_t)(uint32_t)a0.y * (uint32_t)b.y;
-                    acc[0][j][2] += (uint64_t)(uint32_t)a0.z * (uint32_t)b.z;
-                    acc[0][j][3] += (uint64_t)(uint32_t)a0.w * (uint32_t)b.w;
-                    acc[1][j][0] += (uint64_t)(uint32_t)a1.x * (uint32_t)b.x;
-                    acc[1][j][1] += (uint64_t)(uint32_t)a1.y * (uint32_t)b.y;
-                    acc[1][j][2] += (uint64_t)(uint32_t)a1.z * (uint32_t)b.z;
-                    acc[1][j][3] += (uint64_t)(uint32_t)a1.w * (uint32_t)b.w;
+                for (int mt = 0; mt < 2; mt++) {
+                    const int kk = ks * 16 + (mi >> 1) * 8 + r8, mc = wm + 16 * mt + (mi & 1) * 8;
+                    ldsm4t(sA + (a * kKC + kk) * 128 + (((mc >> 3) ^ (kk & 7)) << 4), af[ks][a][mt][0],
+                           af[ks][a][mt][1], af[ks][a][mt][2], af[ks][a][mt][3]);
                 }
-            }
 #pragma unroll
-            for (int i = 0; i < 2; i++)
+        for (int s = 0; s < 7; s++) {
+            float d[2][4][4];
 #pragma unroll
-                for (int j = 0; j < 4; j++)
+            for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-                    for (int x = 0; x < 4; x++)
-                        acc[i][j][x] = (acc[i][j][x] >> 32) * c32[x] + (acc[i][j][x] & 0xffffffffull);
+                for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++) d[mt][nt][i] = 8388608.0f; /* 2^23 */
+#pragma unroll
+            for (int ks = 0; ks < 2; ks++)
+#pragma unroll
+                for (int a = 0; a < 4; a++) {
+                    const int b = s - a;
+                    if (b < 0 || b > 3) continue;
+                    uint32_t bf[4][2];
+#pragma unroll
+                    for (int np2 = 0; np2 < 2; np2++) {
+                        const int kk = ks * 16 + (mi & 1) * 8 + r8, nc = wn + 16 * np2 + (mi >> 1) * 8;
+                        ldsm4t(sB + (b * kKC + kk) * 128 + (((nc >> 3) ^ (kk & 7)) << 4), bf[2 * np2][0],
+                               bf[2 * np2][1], bf[2 * np2 + 1][0], bf[2 * np2 + 1][1]);
+                    }
+#pragma unroll
+                    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                        for (int nt = 0; nt < 4; nt++) mma_bf16(d[mt][nt], af[ks][a][mt], bf[nt][0], bf[nt][1]);
+                }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        acc[mt][nt][i] += (uint64_t)(__float_as_uint(d[mt][nt][i]) & 0x7fffffu) * wt[s];
+        }
+        if ((st % kFoldStages) == kFoldStages - 1) {
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        acc[mt][nt][i] = (acc[mt][nt][i] >> 32) * c32 + (acc[mt][nt][i] & 0xffffffffull);
         }
         __syncthreads(); /* the buffer is restaged by the next iteration */
     }
     cp_async_wait_all();
+    /* the m16n8 accumulator layout: register i of lane (g, tq) is row g + 8 (i / 2), column 2 tq + i % 2 */
+    const int g = lane >> 2, tq = lane & 3;
 #pragma unroll
-    for (int i = 0; i < 2; i++) {
-        const int r = r0 + lane + 32 * i;
+    for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int c = c0 + 4 * w + j;
-            if (r < m && c < n) {
-                int4 o;
-                o.x = (int)reduce64(acc[i][j][0], mods[0], mus[0], c32[0]);
-                o.y = (int)reduce64(acc[i][j][1], mods[1], mus[1], c32[1]);
-                o.z = (int)reduce64(acc[i][j][2], mods[2], mus[2], c32[2]);
-                o.w = (int)reduce64(acc[i][j][3], mods[3], mus[3], c32[3]);
-                WS[((size_t)c * Q + q) * m + r] = o;
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int r = r0 + wm + 16 * mt + g + 8 * (i >> 1), c = c0 + wn + 8 * nt + 2 * tq + (i & 1);
+                if (r < m && c < n) S[((size_t)j * n + c) * m + r] = reduce64(acc[mt][nt][i], md, mu, c32);
             }
-        }
-    }
 }
 
 /* the outputs whose chain stayed in the split form: residues of the sum from
@@ -800,8 +866,7 @@ __global__ void __launch_bounds__(256) gemm_residue_product(int m, int n, int k,
 template <int N>
 __global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alpha, SoA beta, int *cd, int *cs,
                                                            int *ce, er_t *cv, const int *clen, int ldc,
-                                                           const int4 *WS, ChainOut in) {
-    constexpr int Q = N / 4;
+                                                           const uint32_t *S, ChainOut in) {
     const Tables<N> &t = T<N>();
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long mn = (long long)m * n;
@@ -814,24 +879,18 @@ __global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alp
     s.exp = in.exp[e];
     s.ev[0] = in.ev[e];
     s.ev[1] = in.ev[mn + e];
-    const int4 *ws = WS + (size_t)col * Q * m + row;
+    const uint32_t *ws = S + (size_t)col * m + row; /* modulus i at ws[i * m * n] */
     /* D = W * 2^-e: 2^-e from the RNS_POW2 row -e when 0 <= -e <= log2m (a sum's
      * exponent is its smallest product's, so usually), else by squaring */
     const long long ne = -(long long)s.exp;
     const bool row_ok = ne >= 0 && ne <= t.log2m;
     const int *p2 = t.pow2 + (size_t)(row_ok ? ne : 0) * N;
 #pragma unroll
-    for (int q = 0; q < Q; q++) {
-        const int4 v = __ldg(ws + (size_t)q * m);
-        const uint32_t vv[4] = {(uint32_t)v.x, (uint32_t)v.y, (uint32_t)v.z, (uint32_t)v.w};
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int i = 4 * q + j;
-            const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
-            const uint32_t f = row_ok ? (uint32_t)__ldg(p2 + i) : pow2mod(ne, md, mu);
-            const uint32_t d = mulmod(vv[j], f, md, mu);
-            s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
-        }
+    for (int i = 0; i < N; i++) {
+        const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
+        const uint32_t f = row_ok ? (uint32_t)__ldg(p2 + i) : pow2mod(ne, md, mu);
+        const uint32_t d = mulmod(__ldg(ws + (size_t)i * mn), f, md, mu);
+        s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
     }
     const int lenC = __ldg(clen);
     const long long ic = (long long)col * ldc + row;
@@ -862,9 +921,12 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 /* the split form's scratch, carved in this order */
 struct SplitScratch {
-    int4 *wa, *wb, *ws;
+    int4 *wa, *wb;
+    uint16_t *la, *lb; /* limb planes of W(A), W(B) */
+    uint32_t *prod;    /* the modular product, u32 [N][n][m] */
     ChainOut out;
 };
+int round_up(int v, int to) { return (v + to - 1) / to * to; }
 size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp) {
     const size_t mn = (size_t)m * n;
     size_t off = 0;
@@ -875,6 +937,9 @@ size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp
     };
     const size_t wa = take((size_t)m * k * nmod * 4);
     const size_t wb = take((size_t)k * n * nmod * 4);
+    const size_t mp = round_up(m, kTB), np = round_up(n, kTB), kp = round_up(k, kKC);
+    const size_t la = take((size_t)nmod * 4 * kp * mp * 2);
+    const size_t lb = take((size_t)nmod * 4 * kp * np * 2);
     const size_t ws = take(mn * nmod * 4);
     const size_t sg = take(mn * 4);
     const size_t ex = take(mn * 4);
@@ -885,7 +950,9 @@ size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp
         char *p = static_cast<char *>(base);
         sp->wa = reinterpret_cast<int4 *>(p + wa);
         sp->wb = reinterpret_cast<int4 *>(p + wb);
-        sp->ws = reinterpret_cast<int4 *>(p + ws);
+        sp->la = reinterpret_cast<uint16_t *>(p + la);
+        sp->lb = reinterpret_cast<uint16_t *>(p + lb);
+        sp->prod = reinterpret_cast<uint32_t *>(p + ws);
         sp->out = ChainOut{reinterpret_cast<int *>(p + sg), reinterpret_cast<int *>(p + ex),
                            reinterpret_cast<er_t *>(p + ev), reinterpret_cast<int2 *>(p + rd),
                            reinterpret_cast<int *>(p + nr)};
@@ -893,8 +960,8 @@ size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp
     return off;
 }
 
-/* marks: null, or seven events recorded on s before the first launch and
- * after each of the six launches (the phases' times for the probe) */
+/* marks: null, or kGemmSplitPhases + 1 events recorded on s before the first
+ * launch and after each phase (the phases' times for the probe) */
 template <int N>
 cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A, int lda,
                       const mp_array_t &B, int ldb, const mp_array_t &beta, const mp_array_t &C, int ldc,
@@ -904,14 +971,22 @@ cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_arr
     split_scratch(N, m, n, k, ws.ptr, &sp);
     const long long na = (long long)m * k, nb = (long long)k * n, mn = (long long)m * n;
     const long long gx = (m + BX - 1) / BX, gy = (n + BY - 1) / BY;
-    const long long rt = ((long long)m + kRT - 1) / kRT, ct = ((long long)n + kCT - 1) / kCT;
-    if (gx * gy > (1ll << 28) || rt * ct > (1ll << 30) || mn >= (1ll << 31)) return cudaErrorInvalidConfiguration;
+    const int mp = round_up(m, kTB), np = round_up(n, kTB), kp = round_up(k, kKC);
+    const long long tiles = (long long)(mp / kTB) * (np / kTB);
+    const long long la = (long long)mp * kp, lb = (long long)np * kp;
+    if (gx * gy > (1ll << 28) || tiles >= (1ll << 31) || la / 256 >= (1ll << 31) || lb / 256 >= (1ll << 31) ||
+        mn >= (1ll << 31))
+        return cudaErrorInvalidConfiguration;
     constexpr size_t smem = 2 * sizeof(ScalTile<BX, BY>);
+    constexpr int prod_smem = 2 * 2 * 4 * kKC * kTB * 2; /* two stages of A and B limb planes: 64 KB */
     static PerDevice<cudaError_t> attrs(cuda_ok);
     const int dev = current_device();
     cudaError_t e = attrs.get(dev, cudaErrorInvalidDevice, [] {
-        return cudaFuncSetAttribute(gemm_scalar_chain<N, BX, BY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem);
+        cudaError_t r = cudaFuncSetAttribute(gemm_scalar_chain<N, BX, BY>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute(gemm_mma_product, cudaFuncAttributeMaxDynamicSharedMemorySize, prod_smem);
+        return r;
     });
     if (e != cudaSuccess) return e;
     static PerDevice<int> redo_grid([](const int &g) { return g > 0; });
@@ -930,20 +1005,23 @@ cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_arr
     mark(1);
     gemm_prescale_kq<N><<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B.digits, B.sign, B.exp, ldb, k, n, sp.wb);
     mark(2);
+    gemm_limbs<<<(unsigned)((la + 255) / 256), 256, 0, s>>>(sp.wa, m, k, mp, kp, sp.la);
+    gemm_limbs<<<(unsigned)((lb + 255) / 256), 256, 0, s>>>(sp.wb, n, k, np, kp, sp.lb);
+    mark(3);
     gemm_scalar_chain<N, BX, BY><<<(unsigned)(gx * gy), dim3(BX, BY), smem, s>>>(m, n, k, soa(A), lda, soa(B), ldb,
                                                                               sp.out);
-    mark(3);
-    gemm_residue_product<N><<<dim3((unsigned)(rt * ct), N / 4), 256, 0, s>>>(m, n, k, sp.wa, sp.wb, sp.ws);
     mark(4);
+    gemm_mma_product<<<dim3((unsigned)tiles, N), 128, prod_smem, s>>>(m, n, mp, np, kp, sp.la, sp.lb, sp.prod);
+    mark(5);
     er_t *cv = reinterpret_cast<er_t *>(C.eval);
     gemm_split_epilogue<N><<<(unsigned)((mn + 127) / 128), 128, 0, s>>>(m, n, soa(alpha), soa(beta), C.digits, C.sign,
-                                                                         C.exp, cv, C.len, ldc, sp.ws, sp.out);
-    mark(5);
+                                                                         C.exp, cv, C.len, ldc, sp.prod, sp.out);
+    mark(6);
     const long long want = (mn + 127) / 128;
     gemm_redo<N><<<(unsigned)(want < rgrid ? want : rgrid), 128, 0, s>>>(m, n, k, soa(alpha), soa(A), lda, soa(B),
                                                                          ldb, soa(beta), C.digits, C.sign, C.exp, cv,
                                                                          C.len, ldc, sp.wa, sp.wb, sp.out);
-    mark(6);
+    mark(7);
     return cudaGetLastError();
 }
 

@@ -56,9 +56,11 @@ size_t gemm_workspace_bytes(int nmod, int m, int n, int k);
  * that form): W(A), W(B), the modular product and the scalar chain's results,
  * about (mk + kn + mn) * 4n + 48 mn bytes.  A ws of at least this size selects it. */
 size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k);
-/* the split form alone, with marks[0..6] recorded on s before its first launch
- * and after each of its six; cudaErrorNotSupported for another set or a ws too
- * small for that form */
+/* the split form alone, with marks[0..kGemmSplitPhases] recorded on s before
+ * its first launch and after each phase (W(A); W(B); the limb planes; the
+ * scalar chain; the modular product; the epilogue; the per-output chain);
+ * cudaErrorNotSupported for another set or a ws too small for that form */
+constexpr int kGemmSplitPhases = 7;
 cudaError_t launch_gemm_split_marked(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A,
                                      int lda, const mp_array_t &B, int ldb, const mp_array_t &beta,
                                      const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s, cudaEvent_t *marks);

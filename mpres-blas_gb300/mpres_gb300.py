@@ -528,13 +528,13 @@ def gemm(nmod, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, transa=NO_TRANS, tr
                            None, b1x, b1y, g2x, g2y, b3, _stream_handle(stream)), "mpres_gemm")
 
 
-GEMM_PHASES = ("prescale_a", "prescale_b", "scalar_chain", "residue_product", "epilogue", "redo")
+GEMM_PHASES = ("prescale_a", "prescale_b", "limbs", "scalar_chain", "residue_product", "epilogue", "redo")
 
 
 def probe_gemm_phases(nmod, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream=None):
-    """mp_gemm's split form (32 moduli) with each of its six launches timed by
-    events (mpres_probe_gemm_phases): {phase: milliseconds}, GEMM_PHASES order."""
-    ms = (ctypes.c_float * 6)()
+    """mp_gemm's split form (32 moduli) with each of its phases timed by events
+    (mpres_probe_gemm_phases): {phase: milliseconds}, GEMM_PHASES order."""
+    ms = (ctypes.c_float * len(GEMM_PHASES))()
     check(lib().mpres_probe_gemm_phases(nmod, m, n, k, alpha.ref, A.ref, lda, B.ref, ldb, beta.ref, C.ref, ldc, ms,
                                         _stream_handle(stream)), "mpres_probe_gemm_phases")
     return dict(zip(GEMM_PHASES, list(ms)))
