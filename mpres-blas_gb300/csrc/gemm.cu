@@ -748,13 +748,15 @@ __device__ __forceinline__ void cp_async16_cg(uint32_t dst, const void *src) {
  * kTB bf16, 128 bytes, 16-byte chunks XOR-swizzled by row so that ldmatrix reads
  * are free of bank conflicts) come in by cp.async, double buffered (64 KB); a
  * warp keeps the stage's A fragments (all limbs, both k16 steps) in registers
- * and loads B fragments per limb pair.  Output: u32 [32][n][m]. */
+ * and loads B fragments per limb pair.  Output: int4 [n][8][m], modulus j in
+ * component j % 4 of quad j / 4 (the blocks of one tile, j = blockIdx.x, run
+ * side by side, so the four writers of an int4 meet in L2). */
 __global__ void __launch_bounds__(128, 2) gemm_mma_product(int m, int n, int mp, int np, int kp, const uint16_t *LA,
                                                            const uint16_t *LB, uint32_t *S) {
     extern __shared__ __align__(128) unsigned char prod_smem[];
     const Tables<32> &t = T<32>();
-    const int j = blockIdx.y, gx = mp / kTB;
-    const int r0 = (blockIdx.x % gx) * kTB, c0 = (blockIdx.x / gx) * kTB;
+    const int j = blockIdx.x, gx = mp / kTB;
+    const int r0 = (blockIdx.y % gx) * kTB, c0 = (blockIdx.y / gx) * kTB;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int wm = (w & 1) * 32, wn = (w >> 1) * 32;
     const uint32_t md = (uint32_t)t.moduli[j], mu = t.mu[j], c32 = t.pow2_32[j];
@@ -857,7 +859,7 @@ __global__ void __launch_bounds__(128, 2) gemm_mma_product(int m, int n, int mp,
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const int r = r0 + wm + 16 * mt + g + 8 * (i >> 1), c = c0 + wn + 8 * nt + 2 * tq + (i & 1);
-                if (r < m && c < n) S[((size_t)j * n + c) * m + r] = reduce64(acc[mt][nt][i], md, mu, c32);
+                if (r < m && c < n) S[(((size_t)c * 8 + (j >> 2)) * m + r) * 4 + (j & 3)] = reduce64(acc[mt][nt][i], md, mu, c32);
             }
 }
 
@@ -879,18 +881,24 @@ __global__ void __launch_bounds__(128) gemm_split_epilogue(int m, int n, SoA alp
     s.exp = in.exp[e];
     s.ev[0] = in.ev[e];
     s.ev[1] = in.ev[mn + e];
-    const uint32_t *ws = S + (size_t)col * m + row; /* modulus i at ws[i * m * n] */
+    const uint4 *ws = reinterpret_cast<const uint4 *>(S) + (size_t)col * 8 * m + row; /* quad q at ws[q * m] */
     /* D = W * 2^-e: 2^-e from the RNS_POW2 row -e when 0 <= -e <= log2m (a sum's
      * exponent is its smallest product's, so usually), else by squaring */
     const long long ne = -(long long)s.exp;
     const bool row_ok = ne >= 0 && ne <= t.log2m;
     const int *p2 = t.pow2 + (size_t)(row_ok ? ne : 0) * N;
 #pragma unroll
-    for (int i = 0; i < N; i++) {
-        const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
-        const uint32_t f = row_ok ? (uint32_t)__ldg(p2 + i) : pow2mod(ne, md, mu);
-        const uint32_t d = mulmod(__ldg(ws + (size_t)i * mn), f, md, mu);
-        s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
+    for (int q = 0; q < N / 4; q++) {
+        const uint4 v = __ldg(ws + (size_t)q * m);
+        const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int x = 0; x < 4; x++) {
+            const int i = 4 * q + x;
+            const uint32_t md = (uint32_t)t.moduli[i], mu = t.mu[i];
+            const uint32_t f = row_ok ? (uint32_t)__ldg(p2 + i) : pow2mod(ne, md, mu);
+            const uint32_t d = mulmod(vv[x], f, md, mu);
+            s.d[i] = (int)(sg ? (d ? md - d : 0u) : d);
+        }
     }
     const int lenC = __ldg(clen);
     const long long ic = (long long)col * ldc + row;
@@ -923,10 +931,10 @@ size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 struct SplitScratch {
     int4 *wa, *wb;
     uint16_t *la, *lb; /* limb planes of W(A), W(B) */
-    uint32_t *prod;    /* the modular product, u32 [N][n][m] */
+    uint32_t *prod;    /* the modular product, int4 [n][N/4][m] */
     ChainOut out;
 };
-int round_up(int v, int to) { return (v + to - 1) / to * to; }
+long long round_up(long long v, long long to) { return (v + to - 1) / to * to; }
 size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp) {
     const size_t mn = (size_t)m * n;
     size_t off = 0;
@@ -960,6 +968,16 @@ size_t split_scratch(int nmod, int m, int n, int k, void *base, SplitScratch *sp
     return off;
 }
 
+/* shapes whose launch grids and indices the split form's kernels cover (the
+ * others take the tiled lazy chain) */
+bool split_shape_ok(int m, int n, int k) {
+    const long long gx = (m + 31) / 32, gy = (n + 3) / 4;
+    const long long tiles = (round_up(m, kTB) / kTB) * (round_up(n, kTB) / kTB);
+    const long long la = round_up(m, kTB) * round_up(k, kKC), lb = round_up(n, kTB) * round_up(k, kKC);
+    return gx * gy <= (1ll << 28) && tiles <= 65535 && la / 256 < (1ll << 31) && lb / 256 < (1ll << 31) &&
+           (long long)m * n < (1ll << 31);
+}
+
 /* marks: null, or kGemmSplitPhases + 1 events recorded on s before the first
  * launch and after each phase (the phases' times for the probe) */
 template <int N>
@@ -971,12 +989,10 @@ cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_arr
     split_scratch(N, m, n, k, ws.ptr, &sp);
     const long long na = (long long)m * k, nb = (long long)k * n, mn = (long long)m * n;
     const long long gx = (m + BX - 1) / BX, gy = (n + BY - 1) / BY;
-    const int mp = round_up(m, kTB), np = round_up(n, kTB), kp = round_up(k, kKC);
+    const int mp = (int)round_up(m, kTB), np = (int)round_up(n, kTB), kp = (int)round_up(k, kKC);
     const long long tiles = (long long)(mp / kTB) * (np / kTB);
     const long long la = (long long)mp * kp, lb = (long long)np * kp;
-    if (gx * gy > (1ll << 28) || tiles >= (1ll << 31) || la / 256 >= (1ll << 31) || lb / 256 >= (1ll << 31) ||
-        mn >= (1ll << 31))
-        return cudaErrorInvalidConfiguration;
+    if (!split_shape_ok(m, n, k)) return cudaErrorInvalidConfiguration;
     constexpr size_t smem = 2 * sizeof(ScalTile<BX, BY>);
     constexpr int prod_smem = 2 * 2 * 4 * kKC * kTB * 2; /* two stages of A and B limb planes: 64 KB */
     static PerDevice<cudaError_t> attrs(cuda_ok);
@@ -1011,7 +1027,7 @@ cudaError_t run_split(int m, int n, int k, const mp_array_t &alpha, const mp_arr
     gemm_scalar_chain<N, BX, BY><<<(unsigned)(gx * gy), dim3(BX, BY), smem, s>>>(m, n, k, soa(A), lda, soa(B), ldb,
                                                                               sp.out);
     mark(4);
-    gemm_mma_product<<<dim3((unsigned)tiles, N), 128, prod_smem, s>>>(m, n, mp, np, kp, sp.la, sp.lb, sp.prod);
+    gemm_mma_product<<<dim3(N, (unsigned)tiles), 128, prod_smem, s>>>(m, n, mp, np, kp, sp.la, sp.lb, sp.prod);
     mark(5);
     er_t *cv = reinterpret_cast<er_t *>(C.eval);
     gemm_split_epilogue<N><<<(unsigned)((mn + 127) / 128), 128, 0, s>>>(m, n, soa(alpha), soa(beta), C.digits, C.sign,
@@ -1032,7 +1048,7 @@ cudaError_t run(int m, int n, int k, const mp_array_t &alpha, const mp_array_t &
     dim3 block(BX, BY), grid((m + BX - 1) / BX, (n + BY - 1) / BY);
     er_t *cv = reinterpret_cast<er_t *>(C.eval);
     if constexpr (N == 32) {
-        if (ws.ptr != nullptr && ws.bytes >= gemm_split_workspace_bytes(N, m, n, k))
+        if (ws.ptr != nullptr && ws.bytes >= gemm_split_workspace_bytes(N, m, n, k) && split_shape_ok(m, n, k))
             return run_split<N>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s);
     }
     if (ws.ptr != nullptr && ws.bytes >= gemm_workspace_bytes(N, m, n, k)) {
@@ -1068,14 +1084,15 @@ size_t gemm_workspace_bytes(int nmod, int m, int n, int k) {
 }
 
 size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k) {
-    if (nmod != 32) return 0;
+    if (nmod != 32 || !split_shape_ok(m, n, k)) return 0;
     return split_scratch(nmod, m, n, k, nullptr, nullptr);
 }
 
 cudaError_t launch_gemm_split_marked(int nmod, int m, int n, int k, const mp_array_t &alpha, const mp_array_t &A,
                                      int lda, const mp_array_t &B, int ldb, const mp_array_t &beta,
                                      const mp_array_t &C, int ldc, Workspace ws, cudaStream_t s, cudaEvent_t *marks) {
-    if (nmod != 32 || ws.ptr == nullptr || ws.bytes < gemm_split_workspace_bytes(nmod, m, n, k))
+    if (nmod != 32 || ws.ptr == nullptr || ws.bytes < gemm_split_workspace_bytes(nmod, m, n, k) ||
+        !split_shape_ok(m, n, k))
         return cudaErrorNotSupported;
     return run_split<32>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, ws, s, marks);
 }
