@@ -52,9 +52,11 @@ cudaError_t launch_gemv(int nmod, bool trans, int m, int n, const mp_array_t &al
 /* mp_gemm: W(A) and W(B), the signed residues scaled by 2^exp, go to ws
  * (gemm_workspace_bytes); with a smaller ws the chain runs step by step */
 size_t gemm_workspace_bytes(int nmod, int m, int n, int k);
-/* the split form's scratch (32 moduli; 0 for the other sets, which do not take
- * that form): W(A), W(B), the modular product and the scalar chain's results,
- * about (mk + kn + mn) * 4n + 48 mn bytes.  A ws of at least this size selects it. */
+/* the split form's scratch (32 moduli; 0 for the other sets and for shapes
+ * beyond its grids, which do not take that form): W(A), W(B), their bf16 limb
+ * planes, the modular product and the scalar chain's results, about
+ * (mk + kn + mn) * 4n + 8n k'(m' + n') + 48 mn bytes (m', n', k' padded to 64, 64,
+ * 32).  A ws of at least this size selects it. */
 size_t gemm_split_workspace_bytes(int nmod, int m, int n, int k);
 /* the split form alone, with marks[0..kGemmSplitPhases] recorded on s before
  * its first launch and after each phase (W(A); W(B); the limb planes; the
