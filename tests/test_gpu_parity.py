@@ -253,6 +253,19 @@ def test_gemm_without_scratch_vs_oracle(gpu, oracle, monkeypatch, n, lo, hi):
     eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
 
 
+def test_gemm_long_k_vs_oracle(gpu, oracle):
+    """k = 4200 with 32 moduli: the tensor-core modular product folds its 64-bit
+    accumulators every 128 stages of 32 k steps, so this chain crosses a fold
+    (and ends in a partial stage)."""
+    n, m, cols, k = 32, 9, 7, 4200
+    rng = np.random.default_rng(helpers.SEED + 29)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, -32, 32))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, -32, 32))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, -32, 32))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m))
+
+
 def test_gemm_phase_probe_matches_gemm(gpu, oracle):
     """mpres_probe_gemm_phases runs mp_gemm's split form (32 moduli) with an
     event between its launches: the oracle's bits, and a time for each launch."""
