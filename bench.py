@@ -242,11 +242,21 @@ def gemm_roofline(torch, mp, stream, d, c_work, c_init, clocks, step_secs, rates
     inst = entry.get("warp_instructions_per_launch")
     t = phases["scalar_chain"] / 1e3
     achieved = inst / t if inst else None
+    # the second kernel, the modular product, is a bf16 tensor-core kernel: its limb products against the
+    # measured cuBLAS bf16 rate (it runs the legacy mma.sync path)
+    mp_path = ROOT / "MEASURED_PEAKS.json"
+    bf16 = json.loads(mp_path.read_text()).get("bf16_tflops") if mp_path.exists() else None
+    prod_flop = 16.0 * n * 2.0 * m ** 3
+    t_prod = phases["residue_product"] / 1e3
+    product = {"kernel": "gemm_mma_product", "bound": "tensor", "unit": "TFLOP/s", "achieved": prod_flop / t_prod / 1e12,
+               "peak": bf16 or 1900.0, "peak_source": "measured" if bf16 else "fallback",
+               "frac": prod_flop / t_prod / 1e12 / (bf16 or 1900.0), "kernel_ms": phases["residue_product"],
+               "work": "16 bf16 limb products per modulus, %.2f TFLOP" % (prod_flop / 1e12)}
     return {"bound": "int", "kernel": "gemm_scalar_chain", "achieved": achieved / 1e9 if achieved else None,
             "peak": peak / 1e9, "unit": "G warp-instructions/s", "frac": achieved / peak if achieved else None,
             "traffic": entry.get("bytes_per_launch"), "kernel_ms": phases["scalar_chain"],
             "share_of_step": t / step_secs, "phases_ms": phases,
-            "alu_pipe_active": entry.get("alu_pipe_active"),
+            "alu_pipe_active": entry.get("alu_pipe_active"), "product": product,
             "peak_source": "4 warp instructions per cycle per SM x %d SMs x the sampled SM clock" % sms,
             "work_note": "a split-form step: W(A), W(B) and their bf16 limb planes; the scalar chain (sign, "
                          "exponent and interval of every k step, the reference's expressions); the residues as one "

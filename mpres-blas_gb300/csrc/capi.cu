@@ -113,6 +113,15 @@ void fill_tables(const HostTables &h, const int *dpow2, const int *dpow2_inv, co
     for (int i = 0; i < N; i++) t.pow2_32[i] = (uint32_t)((1ull << 32) % (unsigned long long)h.moduli[i]);
     for (int i = 0; i < N; i++)
         t.inv94[i] = (uint64_t)((((unsigned __int128)1) << 94) / (unsigned __int128)(unsigned)h.moduli[i]);
+    for (int i = 0; i < N; i++) { /* (2^-1)^log2m, 2^-1 = (m + 1) / 2 for the odd m */
+        const uint64_t md = (uint64_t)(unsigned)h.moduli[i];
+        uint64_t base = (md + 1) / 2, r = 1;
+        for (unsigned e = (unsigned)h.log2m; e; e >>= 1) {
+            if (e & 1u) r = r * base % md;
+            base = base * base % md;
+        }
+        t.pow2_neg_top[i] = (uint32_t)r;
+    }
     for (int i = 0; i < N; i++) {
         t.recip_rd_m[i] = h.recip_rd_m[i];
         t.recip_ru_m[i] = h.recip_ru_m[i];

@@ -106,12 +106,22 @@ __device__ __forceinline__ uint32_t reduce64(uint64_t v, uint32_t m, uint32_t mu
     return r;
 }
 
-/* W = (-1)^s * d * 2^e mod m_i of one element, for every modulus */
+/* W = (-1)^s * d * 2^e mod m_i of one element, for every modulus.  2^e is the
+ * RNS_POW2 row e for 0 <= e <= log2m, the row e + log2m times 2^-log2m for
+ * -log2m <= e < 0 (the usual case: a converted double's exponent), else by
+ * square and multiply; the same residue every way. */
 template <int N> __device__ __forceinline__ uint32_t encode_residue(int d, int s, long long e, int i) {
     const Tables<N> &t = T<N>();
-    const uint32_t m = (uint32_t)t.moduli[i];
+    const uint32_t m = (uint32_t)t.moduli[i], mu = t.mu[i];
     const uint32_t v = s ? (d ? m - (uint32_t)d : 0u) : (uint32_t)d;
-    return mulmod(v, pow2mod(e, m, t.mu[i]), m, t.mu[i]);
+    uint32_t f;
+    if (e >= 0 && e <= t.log2m)
+        f = (uint32_t)__ldg(t.pow2 + (size_t)e * N + i);
+    else if (e < 0 && e >= -t.log2m)
+        f = mulmod((uint32_t)__ldg(t.pow2 + (size_t)(e + t.log2m) * N + i), t.pow2_neg_top[i], m, mu);
+    else
+        f = pow2mod(e, m, mu);
+    return mulmod(v, f, m, mu);
 }
 
 /* W(A) and W(B): element e (column-major, e = c * rows + r) of a rows x cols

@@ -53,6 +53,7 @@ struct Tables {
     const int *host_ceil_log2;   /* device: host_ceil_log2_table() */
     uint32_t pow2_32[N];         /* 2^32 mod m_i: folds a 64-bit residue accumulator */
     uint64_t inv94[N];           /* floor(2^94 / m_i), 2^63 < inv94 < 2^64: the exact rank shortcut */
+    uint32_t pow2_neg_top[N];    /* 2^-log2m mod m_i: 2^e for -log2m <= e < 0 as an RNS_POW2 row times this */
 };
 
 /* Host-side copy of every table in the reference's array shapes. */
