@@ -711,14 +711,20 @@ int mpres_gemm(int nmod, int transa, int transb, int m, int n, int k, const mp_a
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     Workspace ws;
     /* MPRES_GEMM_NO_SCRATCH=1 selects the step-by-step chain, the path taken when
-     * the workspace cannot grow (same bits, no scratch) */
+     * the workspace cannot grow (same bits, no scratch); MPRES_GEMM_NO_SPLIT=1 the
+     * tiled lazy chain, taken when it can grow to W(A), W(B) but not to the split
+     * form's scratch */
     const char *no_scratch = std::getenv("MPRES_GEMM_NO_SCRATCH");
+    const char *no_split = std::getenv("MPRES_GEMM_NO_SPLIT");
     const bool scratch = !(no_scratch && no_scratch[0] == '1');
+    const bool allow_split = !(no_split && no_split[0] == '1');
     /* the split form's scratch first (32 moduli), else W(A), W(B) alone */
-    const size_t split = scratch ? gemm_split_workspace_bytes(nmod, m, n, k) : 0;
+    const size_t split = scratch && allow_split ? gemm_split_workspace_bytes(nmod, m, n, k) : 0;
     if (scratch && (split == 0 || workspace_grow(s, split, ws) != cudaSuccess) &&
         workspace_grow(s, gemm_workspace_bytes(nmod, m, n, k), ws) != cudaSuccess)
         ws = Workspace{}; /* no room for W(A), W(B): the step-by-step chain, no scratch */
+    if (!allow_split && ws.bytes > gemm_workspace_bytes(nmod, m, n, k))
+        ws.bytes = gemm_workspace_bytes(nmod, m, n, k); /* a stream's workspace may be larger from earlier calls */
     cudaError_t e = launch_gemm(nmod, m, n, k, *alpha, *A, lda, *B, ldb, *beta, *C, ldc, ws, s);
     return e == cudaSuccess ? ok() : cuda_fail(e, "mpres_gemm");
 }

@@ -285,6 +285,23 @@ def test_gemm_phase_probe_matches_gemm(gpu, oracle):
         gpu.probe_gemm_phases(8, 2, 2, 2, da, dA, 2, dB, 2, db, dC, 2)
 
 
+@pytest.mark.parametrize("lo,hi", [(-32, 32), (-400, 400)])
+def test_gemm_tiled_form_vs_oracle(gpu, oracle, monkeypatch, lo, hi):
+    """MPRES_GEMM_NO_SPLIT=1 selects, for 32 moduli, the tiled lazy-residue chain
+    that mp_gemm takes when its workspace can hold W(A), W(B) but not the split
+    form's scratch: the same bits as the split form and the oracle."""
+    n, m, cols, k = 32, 45, 19, 70
+    rng = np.random.default_rng(helpers.SEED + 31 + hi)
+    A = gpu.set_d(n, helpers.doubles(rng, m * k, lo, hi))
+    B = gpu.set_d(n, helpers.doubles(rng, k * cols, lo, hi))
+    C = gpu.set_d(n, helpers.doubles(rng, m * cols, lo, hi))
+    al, be = gpu.set_d(n, rng.uniform(-1, 1, 1)), gpu.set_d(n, rng.uniform(-1, 1, 1))
+    want = oracle.gemm(n, m, cols, k, al, A, m, B, k, be, C, m)
+    eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
+    monkeypatch.setenv("MPRES_GEMM_NO_SPLIT", "1")
+    eq(run_gemm(gpu, n, m, cols, k, al, A, m, B, k, be, C, m), want)
+
+
 def test_gemm_transposed_is_not_supported(gpu):
     rec = gpu.set_d(8, np.ones(4))
     d = gpu.DeviceArray.from_host(8, rec)
