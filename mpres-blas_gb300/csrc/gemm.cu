@@ -102,164 +102,6 @@ __global__ void __launch_bounds__(256) gemm_prescale(const int *digits, const in
 }
 
 
-/* ------------- the scalar half of a step with 32-bit exponents --------------
- *
- * The same values as er_md / er_add / add_scalars / needs_round with the
- * exponents held in 32-bit integers: identical values as long as nothing
- * overflows, which the callers guarantee by taking this form only when every
- * exponent entering the step is within +-2^27 (the operands' exponents within
- * +-2^26): then no intermediate exceeds 2^30 in magnitude.  Half the integer
- * instructions and registers of the 64-bit forms in the hot loop. */
-struct er32 {
-    double frac;
-    int exp;
-};
-struct Scal32 {
-    int sign, exp;
-    er32 ev[2];
-};
-constexpr int kExp32 = 1 << 27;
-__device__ __forceinline__ bool fits32(long long e, int lim) { return e >= -lim && e <= lim; }
-
-__device__ __forceinline__ void er_adjust32(er32 &x) {
-    const uint64_t u = dbits(x.frac);
-    const bool nz = (u << 1) != 0;
-    const int e = x.exp + (int)((u >> 52) & 2047) - 1023;
-    x.exp = nz ? e : 0;
-    x.frac = nz ? bdbl((u & kZeroExpMask) | kBiasExpMask) : bdbl(u & kSign);
-}
-
-template <bool UP> __device__ __forceinline__ er32 er_add32(const er32 &x, const er32 &y) {
-    const bool xnz = dnz(x.frac), ynz = dnz(y.frac);
-    const int xe = xnz ? x.exp : 0, ye = ynz ? y.exp : 0;
-    const int dexp = (xnz && ynz) ? xe - ye : 0;
-    const bool swap = dexp < 0;
-    const double big = swap ? y.frac : x.frac, small = swap ? x.frac : y.frac;
-    er32 r;
-    r.exp = dexp != 0 ? (swap ? ye : xe) : (xe == 0 ? ye : xe);
-    r.frac = dadd<UP>(big, scale2(small, swap ? dexp : -dexp));
-    er_adjust32(r);
-    return r;
-}
-
-/* er_md (mp_device.cuh) in the 32-bit exponent form, with the significands'
- * product from one directed FP64 multiplication (er_md's DP form: what
- * __dmul_rd / __dmul_ru compute, correctly rounded, so the same 53 bits and
- * exponent as the integer product) and the division by the unit on the integer
- * pipes.  The GEMM chains are bound by their integer pipe: one FP64 instruction
- * in place of the 106-bit product, its normalisation and rounding (the split
- * form's scalar chain, 1024^3: 19.1 -> 16.0 ms). */
-template <bool UP>
-__device__ __forceinline__ er32 er_md32_dp(const er32 &x, const er32 &y, const er_t &z, double zr, uint64_t zinv) {
-    constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
-    const uint64_t bx = dbits(x.frac), by = dbits(y.frac);
-    const uint32_t ex = (uint32_t)(bx >> 52) & 2047u, ey = (uint32_t)(by >> 52) & 2047u;
-    const uint64_t sgn = (bx ^ by) & kSign;
-    er32 r;
-    if (ex == 1023u && ey == 1023u) {
-        const bool up = UP != (sgn != 0);
-        /* x*y in [1, 4): the significand p and e = 52 + (exponent of the product) */
-        const uint64_t bp = dbits(dmul<UP>(x.frac, y.frac));
-        const uint64_t p = (bp & kMant) | kHidden;
-        const int e = (int)((bp >> 52) & 2047u) - 1023 + 52;
-        const uint64_t bz = dbits(z.frac);
-        const uint64_t mz = (bz & kMant) | kHidden;
-        const int ez = (int)((bz >> 52) & 2047) - 1023;
-        const bool k52 = p >= mz;
-        uint64_t thi, tlo;
-        mul_wide53x64(p, zinv, thi, tlo);
-        uint64_t q = k52 ? thi : ((thi << 1) | (tlo >> 63));
-        uint64_t rem = (k52 ? (p << 52) : (p << 53)) - q * mz;
-        if (rem >= mz) {
-            q++;
-            rem -= mz;
-        }
-        q += (up && rem) ? 1u : 0u;
-        int E = e - 52 - ez - (k52 ? 52 : 53);
-        if (q >> 53) {
-            q >>= 1;
-            E++;
-        }
-        r.exp = x.exp + y.exp - (int)z.exp + E + 52;
-        r.frac = bdbl(sgn | kBiasExpMask | (q & kMant));
-        return r;
-    }
-    if (((bx << 1) == 0 && ey != 2047u) || ((by << 1) == 0 && ex != 2047u)) {
-        r.exp = 0;
-        r.frac = bdbl(sgn);
-        return r;
-    }
-    r.exp = x.exp + y.exp - (int)z.exp;
-    r.frac = div_by_const<UP>(dmul<UP>(x.frac, y.frac), z.frac, zr);
-    er_adjust32(r);
-    return r;
-}
-
-template <int N> __device__ __forceinline__ bool needs_round32(const er32 &u) {
-    const Tables<N> &t = T<N>();
-    return dnz(u.frac) && u.exp >= t.mp_h; /* then u.exp - mp_h + 1 > 0 as well */
-}
-
-template <int N>
-__device__ __forceinline__ bool add_scalars32(Scal32 &r, int &nzx_out, int &nzy_out, const Scal32 &x, const Scal32 &y) {
-    const Tables<N> &t = T<N>();
-    int ex = x.exp, ey = y.exp, sx = x.sign, sy = y.sign;
-    const int dexp = ex - ey;
-    int gamma = dexp > 0 ? dexp : 0;
-    int theta = dexp < 0 ? -dexp : 0;
-    const int nzx = (!dnz(y.ev[1].frac) || (theta + y.ev[1].exp) < t.mp_j);
-    const int nzy = (!dnz(x.ev[1].frac) || (gamma + x.ev[1].exp) < t.mp_j);
-    gamma *= nzy;
-    theta *= nzx;
-    ex = (ex - gamma) * nzx;
-    ey = (ey - theta) * nzy;
-    sx *= nzx;
-    sy *= nzy;
-    const int fx = (1 - 2 * sx) * nzx;
-    const int fy = (1 - 2 * sy) * nzy;
-    er32 ax[2], ay[2];
-    ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
-    ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
-    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
-    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
-    er32 ev[2];
-    ev[0] = er_add32<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
-    ev[1] = er_add32<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
-    const int sign = dneg(ev[0].frac);
-    const bool decided = sign == (int)dneg(ev[1].frac);
-    r.sign = sign;
-    r.exp = (ex == 0) ? ey : ex;
-    if (sign) {
-        r.ev[0].frac = dflip(ev[1].frac); r.ev[0].exp = ev[1].exp;
-        r.ev[1].frac = dflip(ev[0].frac); r.ev[1].exp = ev[0].exp;
-    } else {
-        r.ev[0] = ev[0];
-        r.ev[1] = ev[1];
-    }
-    nzx_out = nzx;
-    nzy_out = nzy;
-    return decided;
-}
-
-/* the 64-bit sum as a Scal32 when every exponent fits the 32-bit form */
-__device__ __forceinline__ bool narrow32(const Scal &x, Scal32 &y) {
-    y.sign = x.sign;
-    y.exp = x.exp;
-    y.ev[0].frac = x.ev[0].frac;
-    y.ev[0].exp = (int)x.ev[0].exp;
-    y.ev[1].frac = x.ev[1].frac;
-    y.ev[1].exp = (int)x.ev[1].exp;
-    return fits32(x.exp, kExp32) && fits32(x.ev[0].exp, kExp32) && fits32(x.ev[1].exp, kExp32);
-}
-__device__ __forceinline__ void widen32(const Scal32 &x, Scal &y) {
-    y.sign = x.sign;
-    y.exp = x.exp;
-    y.ev[0].frac = x.ev[0].frac;
-    y.ev[0].exp = x.ev[0].exp;
-    y.ev[1].frac = x.ev[1].frac;
-    y.ev[1].exp = x.ev[1].exp;
-}
-
 /* ------------------- the k chain with shared-memory k tiles ------------------
  *
  * The lazy-residue chain of gemm_lazy_output (gemm_chain.cuh, which the batch
