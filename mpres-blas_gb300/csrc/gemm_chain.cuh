@@ -156,57 +156,6 @@ struct Scal {
     er_t ev[2];
 };
 
-/* the test of round_if_needed */
-template <int N> __device__ __forceinline__ bool needs_round(const er_t &u) {
-    const Tables<N> &t = T<N>();
-    return dnz(u.frac) && u.exp >= t.mp_h && (int)(u.exp - t.mp_h + 1) > 0;
-}
-
-/* The scalar half of mp_add (mp_device.cuh), the same expressions: the sum's
- * sign, exponent and interval, and the flags that keep or drop each operand.
- * Returns false when the signs of the bounds disagree: the sign then comes from
- * sign_estimate, which needs the residues. */
-template <int N>
-__device__ __forceinline__ bool add_scalars(Scal &r, int &nzx_out, int &nzy_out, const Scal &x, const Scal &y) {
-    const Tables<N> &t = T<N>();
-    int ex = x.exp, ey = y.exp, sx = x.sign, sy = y.sign;
-    const int dexp = ex - ey;
-    int gamma = dexp > 0 ? dexp : 0;
-    int theta = dexp < 0 ? -dexp : 0;
-    const int nzx = (!dnz(y.ev[1].frac) || (theta + y.ev[1].exp) < t.mp_j);
-    const int nzy = (!dnz(x.ev[1].frac) || (gamma + x.ev[1].exp) < t.mp_j);
-    gamma *= nzy;
-    theta *= nzx;
-    ex = (ex - gamma) * nzx;
-    ey = (ey - theta) * nzy;
-    sx *= nzx;
-    sy *= nzy;
-    const int fx = (1 - 2 * sx) * nzx;
-    const int fy = (1 - 2 * sy) * nzy;
-    er_t ax[2], ay[2];
-    ax[0].exp = x.ev[0].exp + gamma; ax[1].exp = x.ev[1].exp + gamma;
-    ay[0].exp = y.ev[0].exp + theta; ay[1].exp = y.ev[1].exp + theta;
-    ax[0].frac = dscale_sign(x.ev[0].frac, fx); ax[1].frac = dscale_sign(x.ev[1].frac, fx);
-    ay[0].frac = dscale_sign(y.ev[0].frac, fy); ay[1].frac = dscale_sign(y.ev[1].frac, fy);
-    er_t ev[2];
-    ev[0] = er_add<false>(sx ? ax[1] : ax[0], sy ? ay[1] : ay[0]);
-    ev[1] = er_add<true>(sx ? ax[0] : ax[1], sy ? ay[0] : ay[1]);
-    const int sign = dneg(ev[0].frac);
-    const bool decided = sign == (int)dneg(ev[1].frac);
-    r.sign = sign;
-    r.exp = (ex == 0) ? ey : ex;
-    if (sign) {
-        r.ev[0].frac = dflip(ev[1].frac); r.ev[0].exp = ev[1].exp;
-        r.ev[1].frac = dflip(ev[0].frac); r.ev[1].exp = ev[0].exp;
-    } else {
-        r.ev[0] = ev[0];
-        r.ev[1] = ev[1];
-    }
-    nzx_out = nzx;
-    nzy_out = nzy;
-    return decided;
-}
-
 /* the residues D = (-1)^s * W * 2^-e mod m_i of a number from its accumulators */
 template <int N> __device__ __noinline__ void residues_from_acc(int *d, const uint64_t *w, int s, int e) {
     const Tables<N> &t = T<N>();

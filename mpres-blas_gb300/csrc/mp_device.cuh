@@ -281,11 +281,7 @@ __device__ __forceinline__ void mul_wide53x64(uint64_t a, uint64_t b, uint64_t &
     hi = (uint64_t)a1 * b1 + (mid2 >> 32) + carry;
 }
 
-/* DP: the 53-bit product p from one directed FP64 multiplication instead (the
- * value __dmul_rd / __dmul_ru give, correctly rounded like the integer form):
- * fewer integer instructions and one FP64 one, for kernels whose integer pipe
- * is the busy one and whose chains have other warps to hide the FP64 latency. */
-template <bool UP, bool DP = false>
+template <bool UP>
 __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &z, double zr, uint64_t zinv) {
     constexpr uint64_t kMant = (1ull << 52) - 1, kHidden = 1ull << 52;
     const uint64_t bx = dbits(x.frac), by = dbits(y.frac);
@@ -294,25 +290,16 @@ __device__ __forceinline__ er_t er_md(const er_t &x, const er_t &y, const er_t &
     er_t r;
     if (ex == 1023u && ey == 1023u) {
         const bool up = UP != (sgn != 0); /* round the magnitude up */
-        uint64_t p;
-        int e; /* the product is p * 2^(e - 104) */
-        if (DP) {
-            /* x*y in [1, 4): the significand and e = 52 + the product's exponent */
-            const uint64_t bp = dbits(dmul<UP>(x.frac, y.frac));
-            p = (bp & kMant) | kHidden;
-            e = (int)((bp >> 52) & 2047u) - 1023 + 52;
-        } else {
-            const uint64_t mx = (bx & kMant) | kHidden, my = (by & kMant) | kHidden;
-            uint64_t hi, lo;
-            mul_wide53(mx, my, hi, lo); /* P in [2^104, 2^106) */
-            const int sh = (hi >> 41) ? 53 : 52;
-            p = (hi << (64 - sh)) | (lo >> sh);
-            p += (up && (lo & ((1ull << sh) - 1))) ? 1u : 0u;
-            e = sh;
-            if (p >> 53) {
-                p >>= 1;
-                e++;
-            }
+        const uint64_t mx = (bx & kMant) | kHidden, my = (by & kMant) | kHidden;
+        uint64_t hi, lo;
+        mul_wide53(mx, my, hi, lo); /* P in [2^104, 2^106) */
+        const int sh = (hi >> 41) ? 53 : 52;
+        uint64_t p = (hi << (64 - sh)) | (lo >> sh);
+        p += (up && (lo & ((1ull << sh) - 1))) ? 1u : 0u;
+        int e = sh; /* the product is p * 2^(e - 104) */
+        if (p >> 53) {
+            p >>= 1;
+            e++;
         }
         const uint64_t bz = dbits(z.frac);
         const uint64_t mz = (bz & kMant) | kHidden;
