@@ -229,10 +229,9 @@ template <bool UP> __device__ __forceinline__ er32 er_add32(const er32 &x, const
 }
 
 /* er_md (mp_device.cuh) in the 32-bit exponent form, with the significands'
- * product from one directed FP64 multiplication (er_md's DP form: what
- * __dmul_rd / __dmul_ru compute, correctly rounded, so the same 53 bits and
- * exponent as the integer product) and the division by the unit on the integer
- * pipes.  The GEMM chains are bound by their integer pipe: one FP64 instruction
+ * product from one directed FP64 multiplication (what __dmul_rd / __dmul_ru
+ * compute, correctly rounded, so the same 53 bits and exponent as er_md's
+ * integer product) and the division by the unit on the integer pipes as there.  The GEMM chains are bound by their integer pipe: one FP64 instruction
  * in place of the 106-bit product, its normalisation and rounding (the split
  * form's scalar chain, 1024^3: 19.1 -> 16.0 ms). */
 template <bool UP>
